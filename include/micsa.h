@@ -1,0 +1,122 @@
+/*
+ * micsa.h -- C ABI of libmicsa, the GB300 (sm_103a) drop-in for the
+ * microcanonical simulated-annealing sweep of IsidoroGlez/micSA-EA-MC.
+ *
+ * The reference drives its GPU through a handful of host functions that
+ * communicate via globals (PROGRAM/src/main.cu:197-543).  Each entry point
+ * below replaces one of them with explicit state (a micsa_ctx), plain
+ * pointers and sizes, and an int status (MICSA_OK == 0) instead of exit().
+ * Buffers passed in or out use the reference's host layouts, so a caller
+ * that already builds those arrays can switch without re-packing:
+ *
+ *   H            = (L/4)^3 / 2, words per colour of the reference MSC layout
+ *   spins        even[h*nr + r], odd[h*nr + r]            (h_MSC_u_even/odd)
+ *   couplings    J[(p*6 + d)*H + h], d = E,N,U,O,S,D      (viciniB/N[h].J[d])
+ *   demons       w[((p*nc + ic)*H + h)*nr + r]            (CPUwalker0/1)
+ *   LUT          4096-byte s_lut_heat_bath (header.h:113-116)
+ *
+ * On the device the library keeps its own layout (replicas bit-packed in
+ * 32-bit words, colour-split lattice); conversion happens on the GPU.
+ * Calls on one context must come from one thread at a time.  All device work
+ * is issued on the context's own stream; calls that return data to the host
+ * synchronise that stream.
+ */
+#ifndef MICSA_H
+#define MICSA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MICSA_OK 0
+#define MICSA_ERR_ARG 1         /* invalid argument or configuration */
+#define MICSA_ERR_CUDA 2        /* CUDA runtime error (message via micsa_last_error) */
+#define MICSA_ERR_NOMEM 3       /* host or device allocation failed */
+#define MICSA_ERR_STATE 4       /* call not valid in the context's current state */
+#define MICSA_ERR_UNSUPPORTED 5 /* configuration outside what this build supports */
+
+#define MICSA_MAX_SAMPLES 64    /* samples per context (reference: MAXNSAMPLES) */
+
+typedef struct micsa_ctx micsa_ctx;
+
+typedef struct {
+  int device;   /* CUDA device ordinal (argv[7], main.cu:39,52-59) */
+  int L;        /* lattice side: multiple of 8, 8..1024 (header.h:38-40) */
+  int nr;       /* replicas per sample, multiple of 32 (header.h:17 NR) */
+  int nsamples; /* samples simulated together, 1..64 (nbits, main.cu:64) */
+  int nc;       /* demons per site, 1..6 (input.in line 6; d_Walk limit main.cu:1082) */
+} micsa_config;
+
+/* Create a context and allocate its device state.
+ * Replaces CopyDataOnDevice's allocations (main.cu:404-471) and mmcuda
+ * (main.cu:1219-1289). */
+int micsa_create(const micsa_config *cfg, micsa_ctx **out);
+/* Free everything (FreeDevice, main.cu:508-528). NULL is accepted. */
+int micsa_destroy(micsa_ctx *ctx);
+/* Message describing the last failure on this context (never NULL). */
+const char *micsa_last_error(const micsa_ctx *ctx);
+/* Device bytes held by a context of this configuration (for admission). */
+int64_t micsa_footprint_bytes(const micsa_config *cfg);
+
+/* Heat-bath LUT for the Metropolis branch (CopyConstOnDevice,
+ * main.cu:395-397).  bytes must be 4096. */
+int micsa_set_lut(micsa_ctx *ctx, const void *lut, size_t bytes);
+
+/* Couplings of one sample, reference layout (CopyDataOnDevice,
+ * main.cu:436-455). */
+int micsa_upload_couplings(micsa_ctx *ctx, int sample, const uint64_t *J);
+/* Spins of one sample, reference layout (CopyDataOnDevice, main.cu:429-434). */
+int micsa_upload_spins(micsa_ctx *ctx, int sample, const uint64_t *even,
+                       const uint64_t *odd);
+/* Demons of one sample, CPUwalker layout; resets that sample's demon walk
+ * (refresh_walkers, main.cu:340-366). */
+int micsa_upload_demons(micsa_ctx *ctx, int sample, const uint64_t *w0,
+                        const uint64_t *w1);
+
+/* One iteration of Monte_Carlo (main.cu:197-313) on all samples.
+ *   flag = 1: nc x (even, odd) microcanonical half-sweeps, then the demon
+ *             walk.  te and keys are ignored (may be NULL).
+ *   flag = 0: Metropolis even then odd half-sweep with Philox4x32-10 heat-bath
+ *             bits; te holds the two counters produced by _fill_bits
+ *             (fill_bits.h:47-68) for parity 0 then 1: te[(par*nr + r)*4 + k],
+ *             keys[r] the per-replica Philox keys (seed_keys). */
+int micsa_monte_carlo(micsa_ctx *ctx, int flag, const uint32_t *te,
+                      const uint32_t *keys);
+/* n microcanonical iterations back to back (flag = 1 each), replayed from a
+ * CUDA graph of one iteration.  Asynchronous. */
+int micsa_iterate(micsa_ctx *ctx, int64_t n);
+
+/* Measurements of every sample at the current state (Measure_Energy_Spins
+ * main.cu:315-336, Measure_Energy_Clerics med.c:55-83).  Any output may be
+ * NULL.  Layouts:
+ *   e_spin [s*nr + r]  = sum over bonds of J s s  (h_Ener; -e_spin/V is E_s)
+ *   e_demon[s*nr + r]  = sum over sites and demons of D (ener_C)
+ *   q      [s*(nr/2) + k]  overlap of replicas 2k, 2k+1: sum_x s^a_x s^b_x
+ *   c4     [((s*(nr/2) + k)*3 + axis)*(L/2+1) + d] = sum_x q_x q_{x + d e_axis}
+ * q and c4 have no counterpart in the reference. */
+int micsa_measure(micsa_ctx *ctx, int32_t *e_spin, uint64_t *e_demon,
+                  int64_t *q, int64_t *c4);
+
+/* State of one sample back in the reference layouts (copy_from_GPU_for_write,
+ * main.cu:473-490).  Demons are returned in the frame of the current walk. */
+int micsa_download_spins(micsa_ctx *ctx, int sample, uint64_t *even,
+                         uint64_t *odd);
+int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0,
+                          uint64_t *w1);
+
+/* Wait for all work issued on the context (cudaDeviceSynchronize,
+ * main.cu:144,149) and report any asynchronous error. */
+int micsa_synchronize(micsa_ctx *ctx);
+/* Number of kernels this context has launched so far (graph replays count
+ * each kernel node). */
+int64_t micsa_kernel_launches(const micsa_ctx *ctx);
+/* The context's CUDA stream, as a void* (cudaStream_t). */
+void *micsa_stream(micsa_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,454 @@
+/*
+ * C ABI of libmicsa (include/micsa.h): context lifetime, reference-layout
+ * uploads and downloads, the Monte_Carlo step, graph-replayed iterations
+ * and measurements.  Every CUDA call is checked; failures are reported as a
+ * status code plus a message, never by exiting.
+ */
+#include <cuda_runtime.h>
+
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+#include <vector>
+
+#include "micsa.h"
+#include "micsa_kernels.cuh"
+
+struct micsa_ctx {
+  micsa_config cfg;
+  micsa_geo g;
+  cudaStream_t stream = nullptr;
+  uint32_t *spin = nullptr, *dem0 = nullptr, *dem1 = nullptr, *rnd = nullptr;
+  uint8_t *jb = nullptr, *lut = nullptr;
+  uint32_t *te = nullptr, *keys = nullptr;
+  int *walk = nullptr;
+  uint64_t *stage = nullptr;
+  unsigned long long *acc = nullptr;
+  size_t stage_words = 0, acc_words = 0;
+  int have_lut = 0;
+  std::vector<int> have_j, have_spin, have_dem;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t launches = 0;
+  char err[512] = {0};
+};
+
+namespace {
+
+int fail(micsa_ctx *c, int code, const char *fmt, ...) {
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof c->err, fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+#define MICSA_CK(call)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(ctx, MICSA_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                              \
+  } while (0)
+
+struct sizes {
+  int64_t P, H, spin_w, dem_w, rnd_w, jb_b, stage_w, acc_w;
+};
+
+sizes sizes_of(const micsa_config &c) {
+  sizes s;
+  const int64_t L = c.L, W = c.nr / 32;
+  s.P = L * L * L / 2;
+  s.H = (L / 4) * (L / 4) * (L / 4) / 2;
+  s.spin_w = (int64_t)c.nsamples * 2 * s.P * W;
+  s.dem_w = (int64_t)c.nsamples * 2 * c.nc * s.P * W;
+  s.rnd_w = 3 * s.P * W;
+  s.jb_b = (int64_t)c.nsamples * 2 * s.P;
+  const int64_t st_spin = 2 * s.H * c.nr, st_dem = 2 * (int64_t)c.nc * s.H * c.nr;
+  s.stage_w = st_spin > st_dem ? st_spin : st_dem;
+  const int64_t nd = L / 2 + 1, npair = c.nr / 2;
+  s.acc_w = (int64_t)c.nsamples * (2 * c.nr + npair + npair * 3 * nd);
+  return s;
+}
+
+int check_cfg(const micsa_config *c, char *msg, size_t n) {
+  if (!c) return snprintf(msg, n, "null configuration"), MICSA_ERR_ARG;
+  if (c->L < 8 || c->L > 1024 || c->L % 8)
+    return snprintf(msg, n, "L=%d must be a multiple of 8 in [8, 1024]", c->L), MICSA_ERR_ARG;
+  if (c->nr < 32 || c->nr % 32)
+    return snprintf(msg, n, "nr=%d must be a positive multiple of 32", c->nr),
+           MICSA_ERR_UNSUPPORTED;
+  if (c->nsamples < 1 || c->nsamples > MICSA_MAX_SAMPLES)
+    return snprintf(msg, n, "nsamples=%d must be in [1, %d]", c->nsamples, MICSA_MAX_SAMPLES),
+           MICSA_ERR_ARG;
+  if (c->nc < 1 || c->nc > 6)
+    return snprintf(msg, n, "nc=%d must be in [1, 6]", c->nc), MICSA_ERR_ARG;
+  return MICSA_OK;
+}
+
+/* block-edge rotations of a reference word toward -x, -y, -z (RotateO/S/D,
+ * main.cu:732-742): bit of block b receives the bit of block b-1 along the
+ * axis. */
+uint64_t rot_back(int d, uint64_t v) {
+  switch (d) {
+    case 3: { const uint64_t m = 0x8888888888888888ULL; return ((v & m) >> 3) | ((v & ~m) << 1); }
+    case 4: { const uint64_t m = 0xF000F000F000F000ULL; return ((v & m) >> 12) | ((v & ~m) << 4); }
+    default: { const uint64_t m = 0xFFFF000000000000ULL; return ((v & m) >> 48) | ((v & ~m) << 16); }
+  }
+}
+
+int set_device(micsa_ctx *ctx) {
+  MICSA_CK(cudaSetDevice(ctx->cfg.device));
+  return MICSA_OK;
+}
+
+int check_sample(micsa_ctx *ctx, int sample) {
+  if (sample < 0 || sample >= ctx->cfg.nsamples)
+    return fail(ctx, MICSA_ERR_ARG, "sample %d out of range [0, %d)", sample, ctx->cfg.nsamples);
+  return MICSA_OK;
+}
+
+int ensure_stage(micsa_ctx *ctx) {
+  if (ctx->stage) return MICSA_OK;
+  MICSA_CK(cudaMalloc(&ctx->stage, ctx->stage_words * sizeof(uint64_t)));
+  return MICSA_OK;
+}
+
+int ready_for_sweeps(micsa_ctx *ctx, int need_demons) {
+  for (int s = 0; s < ctx->cfg.nsamples; s++) {
+    if (!ctx->have_j[s] || !ctx->have_spin[s])
+      return fail(ctx, MICSA_ERR_STATE, "sample %d has no couplings or spins uploaded", s);
+    if (need_demons && !ctx->have_dem[s])
+      return fail(ctx, MICSA_ERR_STATE, "sample %d has no demons uploaded", s);
+  }
+  return MICSA_OK;
+}
+
+int enqueue_micsa_iteration(micsa_ctx *ctx) {
+  const micsa_geo &g = ctx->g;
+  for (int ic = 0; ic < g.nc; ic++)
+    for (int p = 0; p < 2; p++)
+      MICSA_CK(micsa_launch_sweep_micsa(g, p, ic, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
+                                        ctx->walk, ctx->stream));
+  MICSA_CK(micsa_launch_walk_advance(g, ctx->walk, ctx->stream));
+  return MICSA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t micsa_footprint_bytes(const micsa_config *cfg) {
+  char msg[128];
+  if (check_cfg(cfg, msg, sizeof msg) != MICSA_OK) return -1;
+  sizes s = sizes_of(*cfg);
+  return 4 * (s.spin_w + 2 * s.dem_w + s.rnd_w) + s.jb_b + 8 * (s.stage_w + s.acc_w) + 4096 +
+         4 * (9 * (int64_t)cfg->nr) + 4 * MICSA_MAX_SAMPLES;
+}
+
+int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
+  if (!out) return MICSA_ERR_ARG;
+  *out = nullptr;
+  char msg[256];
+  int rc = check_cfg(cfg, msg, sizeof msg);
+  if (rc != MICSA_OK) {
+    fprintf(stderr, "micsa_create: %s\n", msg);
+    return rc;
+  }
+  micsa_ctx *ctx = new (std::nothrow) micsa_ctx();
+  if (!ctx) return MICSA_ERR_NOMEM;
+  ctx->cfg = *cfg;
+  sizes s = sizes_of(*cfg);
+  micsa_geo &g = ctx->g;
+  g.L = cfg->L;
+  g.Lh = cfg->L / 2;
+  g.W = cfg->nr / 32;
+  g.nc = cfg->nc;
+  g.ns = cfg->nsamples;
+  g.nr = cfg->nr;
+  g.P = s.P;
+  g.H = s.H;
+  ctx->stage_words = (size_t)s.stage_w;
+  ctx->acc_words = (size_t)s.acc_w;
+  ctx->have_j.assign(cfg->nsamples, 0);
+  ctx->have_spin.assign(cfg->nsamples, 0);
+  ctx->have_dem.assign(cfg->nsamples, 0);
+  *out = ctx;
+#define MICSA_CK_CREATE(call)                                                  \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      fprintf(stderr, "micsa_create: %s: %s\n", #call, cudaGetErrorString(e_)); \
+      micsa_destroy(ctx);                                                      \
+      *out = nullptr;                                                          \
+      return e_ == cudaErrorMemoryAllocation ? MICSA_ERR_NOMEM : MICSA_ERR_CUDA; \
+    }                                                                          \
+  } while (0)
+  MICSA_CK_CREATE(cudaSetDevice(cfg->device));
+  MICSA_CK_CREATE(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->spin, 4 * s.spin_w));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->dem0, 4 * s.dem_w));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->dem1, 4 * s.dem_w));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->rnd, 4 * s.rnd_w));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->jb, s.jb_b));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->lut, 4096));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->te, 4 * 8 * (size_t)cfg->nr));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->keys, 4 * (size_t)cfg->nr));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->walk, sizeof(int) * MICSA_MAX_SAMPLES));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->acc, 8 * ctx->acc_words));
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->walk, 0, sizeof(int) * MICSA_MAX_SAMPLES, ctx->stream));
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->spin, 0, 4 * s.spin_w, ctx->stream));
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem0, 0, 4 * s.dem_w, ctx->stream));
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem1, 0, 4 * s.dem_w, ctx->stream));
+  MICSA_CK_CREATE(cudaStreamSynchronize(ctx->stream));
+#undef MICSA_CK_CREATE
+  return MICSA_OK;
+}
+
+int micsa_destroy(micsa_ctx *ctx) {
+  if (!ctx) return MICSA_OK;
+  cudaSetDevice(ctx->cfg.device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  void *bufs[] = {ctx->spin, ctx->dem0, ctx->dem1, ctx->rnd, ctx->jb, ctx->lut,
+                  ctx->te,   ctx->keys, ctx->walk, ctx->stage, ctx->acc};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return MICSA_OK;
+}
+
+const char *micsa_last_error(const micsa_ctx *ctx) { return ctx ? ctx->err : "null context"; }
+
+int64_t micsa_kernel_launches(const micsa_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+void *micsa_stream(micsa_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int micsa_set_lut(micsa_ctx *ctx, const void *lut, size_t bytes) {
+  if (!ctx || !lut) return fail(ctx, MICSA_ERR_ARG, "null argument");
+  if (bytes != 4096) return fail(ctx, MICSA_ERR_ARG, "LUT must be 4096 bytes, got %zu", bytes);
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  MICSA_CK(cudaMemcpyAsync(ctx->lut, lut, 4096, cudaMemcpyHostToDevice, ctx->stream));
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_lut = 1;
+  return MICSA_OK;
+}
+
+int micsa_upload_couplings(micsa_ctx *ctx, int sample, const uint64_t *J) {
+  if (!ctx || !J) return fail(ctx, MICSA_ERR_ARG, "null argument");
+  int rc = check_sample(ctx, sample);
+  if (rc || (rc = set_device(ctx))) return rc;
+  const micsa_geo &g = ctx->g;
+  const int L = g.L, m = L / 4, mh = m / 2;
+  /* per site: bit d = bond in direction d, taken from the reference words
+   * the way d_oneMCstepBN consumes them (main.cu:910-927): forward words
+   * bit-aligned, backward words realigned by the block-edge rotation */
+  std::vector<uint8_t> jb((size_t)(2 * g.P), 0);
+  for (int p = 0; p < 2; p++)
+    for (int64_t h = 0; h < g.H; h++) {
+      const int a2 = (int)(h % mh), b = (int)((h / mh) % m), c = (int)(h / ((int64_t)mh * m));
+      const int a = 2 * a2 + ((b + c + p) & 1);
+      const int wrap[6] = {0, 0, 0, a == 0, b == 0, c == 0};
+      uint64_t w[6];
+      for (int d = 0; d < 6; d++) {
+        w[d] = J[((int64_t)p * 6 + d) * g.H + h];
+        if (wrap[d]) w[d] = rot_back(d, w[d]);
+      }
+      for (int bit = 0; bit < 64; bit++) {
+        const int x = (bit & 3) * m + a, y = ((bit >> 2) & 3) * m + b, z = (bit >> 4) * m + c;
+        uint8_t v = 0;
+        for (int d = 0; d < 6; d++) v |= (uint8_t)(((w[d] >> bit) & 1) << d);
+        jb[(size_t)p * g.P + ((int64_t)z * L + y) * g.Lh + (x >> 1)] = v;
+      }
+    }
+  MICSA_CK(cudaMemcpyAsync(ctx->jb + (int64_t)sample * 2 * g.P, jb.data(), jb.size(),
+                           cudaMemcpyHostToDevice, ctx->stream));
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_j[sample] = 1;
+  return MICSA_OK;
+}
+
+int micsa_upload_spins(micsa_ctx *ctx, int sample, const uint64_t *even, const uint64_t *odd) {
+  if (!ctx || !even || !odd) return fail(ctx, MICSA_ERR_ARG, "null argument");
+  int rc = check_sample(ctx, sample);
+  if (rc || (rc = set_device(ctx)) || (rc = ensure_stage(ctx))) return rc;
+  const micsa_geo &g = ctx->g;
+  const int64_t n = g.H * g.nr;
+  MICSA_CK(cudaMemcpyAsync(ctx->stage, even, 8 * n, cudaMemcpyHostToDevice, ctx->stream));
+  MICSA_CK(cudaMemcpyAsync(ctx->stage + n, odd, 8 * n, cudaMemcpyHostToDevice, ctx->stream));
+  for (int p = 0; p < 2; p++) {
+    MICSA_CK(micsa_launch_from_ref(g, p, 0, 0, ctx->stage + p * n,
+                                   ctx->spin + ((int64_t)sample * 2 + p) * g.P * g.W, ctx->stream));
+    ctx->launches++;
+  }
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_spin[sample] = 1;
+  return MICSA_OK;
+}
+
+int micsa_upload_demons(micsa_ctx *ctx, int sample, const uint64_t *w0, const uint64_t *w1) {
+  if (!ctx || !w0 || !w1) return fail(ctx, MICSA_ERR_ARG, "null argument");
+  int rc = check_sample(ctx, sample);
+  if (rc || (rc = set_device(ctx)) || (rc = ensure_stage(ctx))) return rc;
+  const micsa_geo &g = ctx->g;
+  const int64_t plane = g.H * g.nr, n = 2 * g.nc * plane;
+  const uint64_t *src[2] = {w0, w1};
+  uint32_t *dst[2] = {ctx->dem0, ctx->dem1};
+  for (int k = 0; k < 2; k++) {
+    MICSA_CK(cudaMemcpyAsync(ctx->stage, src[k], 8 * n, cudaMemcpyHostToDevice, ctx->stream));
+    for (int p = 0; p < 2; p++)
+      for (int ic = 0; ic < g.nc; ic++) {
+        const int64_t pi = (int64_t)p * g.nc + ic;
+        MICSA_CK(micsa_launch_from_ref(g, p, ic, 0, ctx->stage + pi * plane,
+                                       dst[k] + ((int64_t)sample * 2 * g.nc + pi) * g.P * g.W,
+                                       ctx->stream));
+        ctx->launches++;
+      }
+  }
+  MICSA_CK(cudaMemsetAsync(ctx->walk + sample, 0, sizeof(int), ctx->stream));
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_dem[sample] = 1;
+  return MICSA_OK;
+}
+
+int micsa_monte_carlo(micsa_ctx *ctx, int flag, const uint32_t *te, const uint32_t *keys) {
+  if (!ctx) return MICSA_ERR_ARG;
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  const micsa_geo &g = ctx->g;
+  if (flag == 1) {
+    if ((rc = ready_for_sweeps(ctx, 1))) return rc;
+    if ((rc = enqueue_micsa_iteration(ctx))) return rc;
+    ctx->launches += 2 * g.nc + 1;
+    return MICSA_OK;
+  }
+  if (flag != 0) return fail(ctx, MICSA_ERR_ARG, "flag must be 0 or 1, got %d", flag);
+  if (!te || !keys) return fail(ctx, MICSA_ERR_ARG, "flag 0 needs counters and keys");
+  if (!ctx->have_lut) return fail(ctx, MICSA_ERR_STATE, "no LUT uploaded");
+  if ((rc = ready_for_sweeps(ctx, 0))) return rc;
+  MICSA_CK(cudaMemcpyAsync(ctx->te, te, 4 * 8 * (size_t)g.nr, cudaMemcpyHostToDevice, ctx->stream));
+  MICSA_CK(cudaMemcpyAsync(ctx->keys, keys, 4 * (size_t)g.nr, cudaMemcpyHostToDevice, ctx->stream));
+  for (int p = 0; p < 2; p++) {
+    MICSA_CK(micsa_launch_gen_rnd(g, p, ctx->te + 4 * g.nr * p, ctx->keys, ctx->lut, ctx->rnd,
+                                  ctx->stream));
+    MICSA_CK(micsa_launch_sweep_metropolis(g, p, ctx->spin, ctx->jb, ctx->rnd, ctx->stream));
+  }
+  ctx->launches += 4;
+  return MICSA_OK;
+}
+
+int micsa_iterate(micsa_ctx *ctx, int64_t n) {
+  if (!ctx || n < 0) return fail(ctx, MICSA_ERR_ARG, "bad argument");
+  int rc = set_device(ctx);
+  if (rc || (rc = ready_for_sweeps(ctx, 1))) return rc;
+  if (!ctx->graph_exec) {
+    MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue_micsa_iteration(ctx);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    MICSA_CK(e);
+    ctx->graph = graph;
+    MICSA_CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
+  }
+  for (int64_t i = 0; i < n; i++) MICSA_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+  ctx->launches += n * (2 * ctx->g.nc + 1);
+  return MICSA_OK;
+}
+
+int micsa_measure(micsa_ctx *ctx, int32_t *e_spin, uint64_t *e_demon, int64_t *q, int64_t *c4) {
+  if (!ctx) return MICSA_ERR_ARG;
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  const micsa_geo &g = ctx->g;
+  const int ns = g.ns, nr = g.nr, np = nr / 2, nd = g.L / 2 + 1;
+  unsigned long long *unsat = ctx->acc, *dem = unsat + ns * nr, *qd = dem + ns * nr,
+                     *c4d = qd + ns * np;
+  if (e_spin || e_demon) {
+    if ((rc = ready_for_sweeps(ctx, e_demon != nullptr))) return rc;
+  } else if (q || c4) {
+    if ((rc = ready_for_sweeps(ctx, 0))) return rc;
+  }
+  MICSA_CK(cudaMemsetAsync(ctx->acc, 0, 8 * ctx->acc_words, ctx->stream));
+  if (e_spin) { MICSA_CK(micsa_launch_energy(g, ctx->spin, ctx->jb, unsat, ctx->stream)); ctx->launches++; }
+  if (e_demon) { MICSA_CK(micsa_launch_demon_energy(g, ctx->dem0, ctx->dem1, dem, ctx->stream)); ctx->launches++; }
+  if (q || c4) { MICSA_CK(micsa_launch_overlap(g, ctx->spin, qd, c4d, ctx->stream)); ctx->launches++; }
+  std::vector<unsigned long long> h(ctx->acc_words);
+  MICSA_CK(cudaMemcpyAsync(h.data(), ctx->acc, 8 * ctx->acc_words, cudaMemcpyDeviceToHost, ctx->stream));
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  const int64_t V = 2 * g.P;
+  const unsigned long long *hu = h.data(), *hd = hu + ns * nr, *hq = hd + ns * nr,
+                           *hc = hq + ns * np;
+  for (int i = 0; i < ns * nr; i++) {
+    if (e_spin) e_spin[i] = (int32_t)(3 * V - 2 * (int64_t)hu[i]);
+    if (e_demon) e_demon[i] = hd[i];
+  }
+  for (int i = 0; i < ns * np; i++)
+    if (q) q[i] = V - 2 * (int64_t)hq[i];
+  if (c4)
+    for (int64_t i = 0; i < (int64_t)ns * np * 3 * nd; i++) c4[i] = V - 2 * (int64_t)hc[i];
+  return MICSA_OK;
+}
+
+int micsa_download_spins(micsa_ctx *ctx, int sample, uint64_t *even, uint64_t *odd) {
+  if (!ctx || !even || !odd) return fail(ctx, MICSA_ERR_ARG, "null argument");
+  int rc = check_sample(ctx, sample);
+  if (rc || (rc = set_device(ctx)) || (rc = ensure_stage(ctx))) return rc;
+  const micsa_geo &g = ctx->g;
+  const int64_t n = g.H * g.nr;
+  for (int p = 0; p < 2; p++) {
+    MICSA_CK(micsa_launch_to_ref(g, p, 0, nullptr, sample,
+                                 ctx->spin + ((int64_t)sample * 2 + p) * g.P * g.W,
+                                 ctx->stage + p * n, ctx->stream));
+    ctx->launches++;
+  }
+  MICSA_CK(cudaMemcpyAsync(even, ctx->stage, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  MICSA_CK(cudaMemcpyAsync(odd, ctx->stage + n, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  return MICSA_OK;
+}
+
+int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0, uint64_t *w1) {
+  if (!ctx || !w0 || !w1) return fail(ctx, MICSA_ERR_ARG, "null argument");
+  int rc = check_sample(ctx, sample);
+  if (rc || (rc = set_device(ctx)) || (rc = ensure_stage(ctx))) return rc;
+  const micsa_geo &g = ctx->g;
+  const int64_t plane = g.H * g.nr, n = 2 * g.nc * plane;
+  const uint32_t *src[2] = {ctx->dem0, ctx->dem1};
+  uint64_t *dst[2] = {w0, w1};
+  for (int k = 0; k < 2; k++) {
+    for (int p = 0; p < 2; p++)
+      for (int ic = 0; ic < g.nc; ic++) {
+        const int64_t pi = (int64_t)p * g.nc + ic;
+        MICSA_CK(micsa_launch_to_ref(g, p, ic, ctx->walk, sample,
+                                     src[k] + ((int64_t)sample * 2 * g.nc + pi) * g.P * g.W,
+                                     ctx->stage + pi * plane, ctx->stream));
+        ctx->launches++;
+      }
+    MICSA_CK(cudaMemcpyAsync(dst[k], ctx->stage, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  return MICSA_OK;
+}
+
+int micsa_synchronize(micsa_ctx *ctx) {
+  if (!ctx) return MICSA_ERR_ARG;
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  MICSA_CK(cudaGetLastError());
+  return MICSA_OK;
+}
+
+}  // extern "C"

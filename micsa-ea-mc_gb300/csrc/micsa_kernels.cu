@@ -1,0 +1,563 @@
+/*
+ * sm_103a kernels of libmicsa: the microcanonical (ISI) and Metropolis
+ * checkerboard half-sweeps, the Philox4x32-10 heat-bath bit generator,
+ * reference-layout conversion and the popcount measurements.
+ * Layout and walk convention: see micsa_kernels.cuh.
+ *
+ * All of this is integer/bitwise work bounded by memory bandwidth: every
+ * half-sweep streams one demon plane (read + write) and the spins of both
+ * colours; there is no contraction for tensor cores.
+ */
+#include "micsa_kernels.cuh"
+
+namespace {
+
+constexpr int TPB = 256;
+constexpr unsigned FULL = 0xffffffffu;
+
+/* ---------------------------------------------------------------- vectors */
+template <int VW> struct vt;
+template <> struct vt<1> { typedef uint32_t T; };
+template <> struct vt<2> { typedef uint2 T; };
+template <> struct vt<4> { typedef uint4 T; };
+
+__device__ __forceinline__ void unpack(uint32_t t, uint32_t (&o)[1]) { o[0] = t; }
+__device__ __forceinline__ void unpack(uint2 t, uint32_t (&o)[2]) { o[0] = t.x; o[1] = t.y; }
+__device__ __forceinline__ void unpack(uint4 t, uint32_t (&o)[4]) {
+  o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+}
+__device__ __forceinline__ uint32_t pack(const uint32_t (&o)[1]) { return o[0]; }
+__device__ __forceinline__ uint2 pack(const uint32_t (&o)[2]) { return make_uint2(o[0], o[1]); }
+__device__ __forceinline__ uint4 pack(const uint32_t (&o)[4]) {
+  return make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+/* read-only path (other colour, couplings) */
+template <int VW>
+__device__ __forceinline__ void ld_ro(const uint32_t *p, uint32_t (&o)[VW]) {
+  unpack(__ldg(reinterpret_cast<const typename vt<VW>::T *>(p)), o);
+}
+/* own colour: read then written back by the same thread */
+template <int VW>
+__device__ __forceinline__ void ld_rw(const uint32_t *p, uint32_t (&o)[VW]) {
+  unpack(*reinterpret_cast<const typename vt<VW>::T *>(p), o);
+}
+template <int VW>
+__device__ __forceinline__ void st_rw(uint32_t *p, const uint32_t (&o)[VW]) {
+  *reinterpret_cast<typename vt<VW>::T *>(p) = pack(o);
+}
+/* demon planes: touched once per iteration, streamed (evict-first) */
+template <int VW>
+__device__ __forceinline__ void ld_stream(const uint32_t *p, uint32_t (&o)[VW]) {
+  unpack(__ldcs(reinterpret_cast<const typename vt<VW>::T *>(p)), o);
+}
+template <int VW>
+__device__ __forceinline__ void st_stream(uint32_t *p, const uint32_t (&o)[VW]) {
+  __stcs(reinterpret_cast<typename vt<VW>::T *>(p), pack(o));
+}
+
+/* ------------------------------------------------------------ geometry */
+struct site_xyz { int x, y, z; };
+
+/* real site of the reference word (colour p, h, bit b) (ini.c:317-337) */
+__device__ __forceinline__ site_xyz ref_site(const micsa_geo &g, int p, int64_t h, int b) {
+  const int m = g.L >> 2, mh = m >> 1;
+  const int a2 = (int)(h % mh);
+  const int64_t q = h / mh;
+  const int bb = (int)(q % m);
+  const int c = (int)(q / m);
+  const int a = 2 * a2 + ((bb + c + p) & 1);
+  site_xyz s;
+  s.x = (b & 3) * m + a;
+  s.y = ((b >> 2) & 3) * m + bb;
+  s.z = (b >> 4) * m + c;
+  return s;
+}
+
+/* where the demon of site (x,y,z) is stored after k walks (header note) */
+__device__ __forceinline__ int64_t demon_slot(const micsa_geo &g, int p, int ic, int k,
+                                              int x, int y, int z) {
+  const int L = g.L;
+  const int sh = ((p == 0) == (ic < 3)) ? 2 * k : -2 * k; /* lattice units */
+  const int axis = ic < 3 ? ic : ic - 3;
+  if (axis == 0) { x -= sh; if (x < 0) x += L; else if (x >= L) x -= L; }
+  else if (axis == 1) { y -= sh; if (y < 0) y += L; else if (y >= L) y -= L; }
+  else { z -= sh; if (z < 0) z += L; else if (z >= L) z -= L; }
+  return ((int64_t)z * L + y) * g.Lh + (x >> 1);
+}
+
+__device__ __forceinline__ uint32_t jmask(uint32_t jb, int d) {
+  return 0u - ((jb >> d) & 1u);
+}
+
+/* 32x32 bit transpose across a warp: lane c returns the word whose bit i is
+ * bit c of lane i's input. */
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane) {
+  uint32_t m = 0x0000FFFFu;
+#pragma unroll
+  for (int j = 16; j != 0; j >>= 1, m ^= m << j) {
+    const uint32_t p = __shfl_xor_sync(FULL, x, j);
+    if (lane & j)
+      x ^= ((p >> j) ^ x) & m;
+    else
+      x ^= (((x >> j) ^ p) & m) << j;
+  }
+  return x;
+}
+
+/* --------------------------------------------------------------- sweeps */
+
+/* Microcanonical update with demon D = D0 + 2*D1 and unsatisfied-bond
+ * counts (j1 + 2*j2) + (j3 + 2*j4): the ISI boolean algebra of the
+ * reference (main.cu:1037-1074).  Equivalent to: accept iff
+ * 0 <= D + u - 3 <= 3, then D <- D + u - 3. */
+__device__ __forceinline__ uint32_t isi_update(uint32_t j1, uint32_t j2, uint32_t j3,
+                                               uint32_t j4, uint32_t &D0, uint32_t &D1) {
+  const uint32_t x13 = j1 ^ j3, x24 = j2 ^ j4;
+  const uint32_t sub = (x24 & ~j1 & ~j3) | (~j2 & ~j4);
+  const uint32_t s0 = ~x13;
+  uint32_t s1 = ~x24 & (x13 | (s0 & ~(j1 ^ j2)));
+  s1 = (~sub & s1) | (sub & (s1 ^ s0));
+  const uint32_t n0 = D0 ^ s0, k1 = D0 & s0, k2 = D1 ^ s1, n1 = k1 ^ k2, k3 = D1 & s1;
+  const uint32_t flip = ~((k3 | (k2 & k1)) ^ sub);
+  D0 = (flip & n0) | (~flip & D0);
+  D1 = (flip & n1) | (~flip & D1);
+  return flip;
+}
+
+/* Metropolis acceptance with Bernoulli words (main.cu:945-957). */
+__device__ __forceinline__ uint32_t metropolis_flip(uint32_t j1, uint32_t j2, uint32_t j3,
+                                                    uint32_t j4, uint32_t b0, uint32_t b1,
+                                                    uint32_t b2) {
+  b1 &= b0;
+  b2 &= b1;
+  const uint32_t id2 = b1, id1 = (b0 ^ b1) | b2, j24 = j2 | j4;
+  return (j1 & j3 & id1) | ((j24 | id2) & (j1 | j3 | id1)) | ((j2 & j4) | (j24 & id2));
+}
+
+/* One thread = one site of colour p and VW consecutive replica words of it.
+ * blockIdx.z = sample, blockIdx.y = z plane, x covers (y, x/2, word group). */
+template <int VW, bool MICSA>
+__global__ void __launch_bounds__(TPB)
+k_sweep(const micsa_geo g, const int p, const int ic, const int G,
+        uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
+        uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
+        const int *__restrict__ walk, const uint32_t *__restrict__ rnd) {
+  const int s = blockIdx.z;
+  const int z = blockIdx.y;
+  const int L = g.L, Lh = g.Lh, W = g.W;
+  const int64_t j = (int64_t)blockIdx.x * TPB + threadIdx.x;
+  if (j >= (int64_t)L * Lh * G) return;
+  const int grp = (int)(j % G);
+  const int ps = (int)(j / G);
+  const int y = ps / Lh;
+  const int xh = ps - y * Lh;
+  const int64_t P = g.P;
+
+  const int rowoff = (y + z + p) & 1; /* x = 2*xh + rowoff */
+  int xe = xh + rowoff;
+  if (xe == Lh) xe = 0;
+  int xo = xh + rowoff - 1;
+  if (xo < 0) xo = Lh - 1;
+  const int yp = (y + 1 == L) ? 0 : y + 1, ym = (y == 0) ? L - 1 : y - 1;
+  const int zp = (z + 1 == L) ? 0 : z + 1, zm = (z == 0) ? L - 1 : z - 1;
+  const int64_t row = (int64_t)z * L;
+  const int64_t i = (row + y) * Lh + xh;
+
+  uint32_t *mine = spin + (int64_t)(s * 2 + p) * P * W + grp * VW;
+  const uint32_t *oth = spin + (int64_t)(s * 2 + (p ^ 1)) * P * W + grp * VW;
+
+  uint32_t sv[VW], nE[VW], nN[VW], nU[VW], nO[VW], nS[VW], nD[VW];
+  ld_rw<VW>(mine + i * W, sv);
+  ld_ro<VW>(oth + ((row + y) * Lh + xe) * W, nE);
+  ld_ro<VW>(oth + ((row + yp) * Lh + xh) * W, nN);
+  ld_ro<VW>(oth + (((int64_t)zp * L + y) * Lh + xh) * W, nU);
+  ld_ro<VW>(oth + ((row + y) * Lh + xo) * W, nO);
+  ld_ro<VW>(oth + ((row + ym) * Lh + xh) * W, nS);
+  ld_ro<VW>(oth + (((int64_t)zm * L + y) * Lh + xh) * W, nD);
+  const uint32_t jbits = __ldg(jb + (int64_t)(s * 2 + p) * P + i);
+  const uint32_t m0 = jmask(jbits, 0), m1 = jmask(jbits, 1), m2 = jmask(jbits, 2);
+  const uint32_t m3 = jmask(jbits, 3), m4 = jmask(jbits, 4), m5 = jmask(jbits, 5);
+
+  uint32_t a0[VW], a1[VW], a2[VW];
+  uint32_t *q0 = nullptr, *q1 = nullptr;
+  if (MICSA) {
+    const int64_t slot = demon_slot(g, p, ic, walk[s], 2 * xh + rowoff, y, z);
+    const int64_t base = ((int64_t)(s * 2 + p) * g.nc + ic) * P * W + grp * VW;
+    q0 = d0 + base + slot * W;
+    q1 = d1 + base + slot * W;
+    ld_stream<VW>(q0, a0);
+    ld_stream<VW>(q1, a1);
+  } else {
+    const uint32_t *rb = rnd + i * W + grp * VW;
+    ld_stream<VW>(rb, a0);
+    ld_stream<VW>(rb + P * W, a1);
+    ld_stream<VW>(rb + 2 * P * W, a2);
+  }
+
+#pragma unroll
+  for (int w = 0; w < VW; w++) {
+    const uint32_t sw = sv[w];
+    const uint32_t f0 = sw ^ nE[w] ^ m0, f1 = sw ^ nN[w] ^ m1, f2 = sw ^ nU[w] ^ m2;
+    const uint32_t f3 = sw ^ nO[w] ^ m3, f4 = sw ^ nS[w] ^ m4, f5 = sw ^ nD[w] ^ m5;
+    const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
+    const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+    uint32_t flip;
+    if (MICSA)
+      flip = isi_update(j1, j2, j3, j4, a0[w], a1[w]);
+    else
+      flip = metropolis_flip(j1, j2, j3, j4, a0[w], a1[w], a2[w]);
+    sv[w] = sw ^ flip;
+  }
+  st_rw<VW>(mine + i * W, sv);
+  if (MICSA) {
+    st_stream<VW>(q0, a0);
+    st_stream<VW>(q1, a1);
+  }
+}
+
+/* ------------------------------------------------------ Philox + LUT bits */
+
+/* Philox4x32-10 (Salmon et al., SC'11): 10 rounds, Weyl key schedule. */
+__device__ __forceinline__ void philox10(uint32_t (&v)[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int rd = 0; rd < 10; rd++) {
+    if (rd) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    const uint32_t lo0 = 0xD2511F53u * v[0], hi0 = __umulhi(0xD2511F53u, v[0]);
+    const uint32_t lo1 = 0xCD9E8D57u * v[2], hi1 = __umulhi(0xCD9E8D57u, v[2]);
+    const uint32_t n0 = hi1 ^ v[1] ^ k0, n2 = hi0 ^ v[3] ^ k1;
+    v[0] = n0; v[1] = lo1; v[2] = n2; v[3] = lo0;
+  }
+}
+
+/* first threshold above the 64-bit uniform (hi, lo), with the 10-bit
+ * prebisection table (main.cu:615-630) */
+__device__ __forceinline__ uint32_t lut_bisect(uint32_t hi, uint32_t lo, const uint32_t *thr,
+                                               const uint16_t *pre) {
+#define MICSA_BELOW(ix) ((hi == thr[2 * (ix)]) ? (lo < thr[2 * (ix) + 1]) : (hi < thr[2 * (ix)]))
+  uint32_t a = 255, b = 255;
+  if (MICSA_BELOW(254)) {
+    const uint32_t e = pre[hi >> 22];
+    a = e & 255u;
+    b = e >> 8;
+  }
+  while (b - a > 1) {
+    const uint32_t mid = (a + b) >> 1;
+    if (MICSA_BELOW(mid)) b = mid; else a = mid;
+  }
+  return MICSA_BELOW(a) ? a : b;
+#undef MICSA_BELOW
+}
+
+/* one 32-bit word of Bernoulli bits from one Philox call, with the
+ * reference's counter bump, post-mix and rotation (main.cu:597-644) */
+__device__ __forceinline__ uint32_t heat_bath_word(uint32_t (&c)[4], uint32_t k0, uint32_t k1,
+                                                   const uint32_t *thr, const uint16_t *pre) {
+  uint32_t v[4] = {c[0], c[1], c[2], c[3]};
+  philox10(v, k0, k1);
+  c[0]++;
+  const uint32_t hi = v[0] ^ v[2], lo = v[1] ^ v[3];
+  uint32_t l[4];
+  l[0] = ((v[1] << 17) | (v[0] >> 15)) ^ hi ^ ((hi << 21) | (lo >> 11));
+  l[1] = ((v[0] << 17) | (v[1] >> 15)) ^ lo ^ (lo << 21);
+  l[2] = (hi << 28) | (lo >> 4);
+  l[3] = (lo << 28) | (hi >> 4);
+  const uint32_t rot = (l[0] + v[1] + l[2] + v[3]) >> 27;
+  uint32_t bb = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) bb |= lut_bisect(v[k], l[k], thr, pre) << (8 * k);
+  return __funnelshift_l(bb, bb, rot);
+}
+
+/* Thread (h, r) = tid = h*nr + r, exactly the reference's thread id, key
+ * (tid, keys[r]) and counter te[r] with z += tid; the three 64-bit words
+ * (bit = block) are transposed in-warp to replica words of the 64 sites. */
+__global__ void __launch_bounds__(TPB)
+k_gen_rnd(const micsa_geo g, const int p, const uint32_t *__restrict__ te,
+          const uint32_t *__restrict__ keys, const uint8_t *__restrict__ lut,
+          uint32_t *__restrict__ rnd) {
+  __shared__ uint32_t s_thr[512];
+  __shared__ uint16_t s_pre[1024];
+  const uint32_t *lw = reinterpret_cast<const uint32_t *>(lut);
+  for (int t = threadIdx.x; t < 1024; t += TPB) {
+    const uint32_t v = lw[t];
+    if (t < 512) s_thr[t] = v;
+    else {
+      s_pre[2 * (t - 512)] = (uint16_t)(v & 0xffffu);
+      s_pre[2 * (t - 512) + 1] = (uint16_t)(v >> 16);
+    }
+  }
+  __syncthreads();
+  const int64_t tid = (int64_t)blockIdx.x * TPB + threadIdx.x;
+  if (tid >= g.H * g.nr) return; /* warp-uniform: H*nr is a multiple of 32 */
+  const int lane = threadIdx.x & 31;
+  const int r = (int)(tid % g.nr);
+  const int64_t h = tid / g.nr;
+  uint32_t c[4] = {te[4 * r], te[4 * r + 1], te[4 * r + 2] + (uint32_t)tid, te[4 * r + 3]};
+  const uint32_t key1 = keys[r];
+  uint32_t wd[6];
+#pragma unroll
+  for (int q = 0; q < 6; q++) wd[q] = heat_bath_word(c, (uint32_t)tid, key1, s_thr, s_pre);
+  const site_xyz a = ref_site(g, p, h, lane), b = ref_site(g, p, h, lane + 32);
+  const int64_t ia = ((int64_t)a.z * g.L + a.y) * g.Lh + (a.x >> 1);
+  const int64_t ib = ((int64_t)b.z * g.L + b.y) * g.Lh + (b.x >> 1);
+  const int w = r >> 5;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    /* 64-bit word k = (wd[2k] << 32) | wd[2k+1]; bit b = block b */
+    const uint32_t lo = warp_transpose32(wd[2 * k + 1], lane);
+    const uint32_t hi = warp_transpose32(wd[2 * k], lane);
+    rnd[((int64_t)k * g.P + ia) * g.W + w] = lo;
+    rnd[((int64_t)k * g.P + ib) * g.W + w] = hi;
+  }
+}
+
+__global__ void k_walk_advance(int *walk, int ns, int period) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < ns) {
+    const int k = walk[s] + 1;
+    walk[s] = (k == period) ? 0 : k;
+  }
+}
+
+/* --------------------------------------------------- layout conversion */
+
+/* Warp per (h, word w): lane l reads replica 32w+l of reference word h
+ * (64 sites), the transpose gives lane l the replica word of block l and
+ * block l+32. */
+__global__ void __launch_bounds__(TPB)
+k_from_ref(const micsa_geo g, const int p, const int ic, const int k,
+           const uint64_t *__restrict__ ref, uint32_t *__restrict__ dst) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (TPB / 32);
+  for (int64_t wi = (int64_t)blockIdx.x * (TPB / 32) + (threadIdx.x >> 5); wi < g.H * g.W;
+       wi += nwarps) {
+    const int64_t h = wi / g.W;
+    const int w = (int)(wi % g.W);
+    const uint64_t v = ref[h * g.nr + w * 32 + lane];
+    const uint32_t lo = warp_transpose32((uint32_t)v, lane);
+    const uint32_t hi = warp_transpose32((uint32_t)(v >> 32), lane);
+    const site_xyz a = ref_site(g, p, h, lane), b = ref_site(g, p, h, lane + 32);
+    dst[demon_slot(g, p, ic, k, a.x, a.y, a.z) * g.W + w] = lo;
+    dst[demon_slot(g, p, ic, k, b.x, b.y, b.z) * g.W + w] = hi;
+  }
+}
+
+__global__ void __launch_bounds__(TPB)
+k_to_ref(const micsa_geo g, const int p, const int ic, const int *__restrict__ walk,
+         const int sample, const uint32_t *__restrict__ src, uint64_t *__restrict__ ref) {
+  const int lane = threadIdx.x & 31;
+  const int k = walk ? walk[sample] : 0;
+  const int64_t nwarps = (int64_t)gridDim.x * (TPB / 32);
+  for (int64_t wi = (int64_t)blockIdx.x * (TPB / 32) + (threadIdx.x >> 5); wi < g.H * g.W;
+       wi += nwarps) {
+    const int64_t h = wi / g.W;
+    const int w = (int)(wi % g.W);
+    const site_xyz a = ref_site(g, p, h, lane), b = ref_site(g, p, h, lane + 32);
+    const uint32_t lo = warp_transpose32(src[demon_slot(g, p, ic, k, a.x, a.y, a.z) * g.W + w], lane);
+    const uint32_t hi = warp_transpose32(src[demon_slot(g, p, ic, k, b.x, b.y, b.z) * g.W + w], lane);
+    ref[h * g.nr + w * 32 + lane] = (uint64_t)lo | ((uint64_t)hi << 32);
+  }
+}
+
+/* ---------------------------------------------------------- measurement */
+
+/* Unsatisfied bonds per replica, summed over the 6 bonds of every colour-0
+ * site (each bond has exactly one colour-0 end).  blockIdx.y = word w,
+ * blockIdx.z = sample; warps stride over chunks of 32 sites. */
+__global__ void __launch_bounds__(TPB)
+k_energy(const micsa_geo g, const uint32_t *__restrict__ spin, const uint8_t *__restrict__ jb,
+         unsigned long long *__restrict__ unsat) {
+  const int s = blockIdx.z, w = blockIdx.y, lane = threadIdx.x & 31;
+  const int L = g.L, Lh = g.Lh, W = g.W;
+  const int64_t P = g.P;
+  const uint32_t *mine = spin + (int64_t)(s * 2) * P * W + w;
+  const uint32_t *oth = spin + (int64_t)(s * 2 + 1) * P * W + w;
+  const uint8_t *jbs = jb + (int64_t)(s * 2) * P;
+  unsigned long long acc = 0;
+  const int64_t step = (int64_t)gridDim.x * TPB;
+  for (int64_t base = (int64_t)blockIdx.x * TPB + (threadIdx.x & ~31); base < P; base += step) {
+    const int64_t i = base + lane; /* P is a multiple of 32: all lanes valid */
+    const int xh = (int)(i % Lh);
+    const int64_t q = i / Lh;
+    const int y = (int)(q % L), z = (int)(q / L);
+    const int rowoff = (y + z) & 1;
+    int xe = xh + rowoff; if (xe == Lh) xe = 0;
+    int xo = xh + rowoff - 1; if (xo < 0) xo = Lh - 1;
+    const int yp = (y + 1 == L) ? 0 : y + 1, ym = (y == 0) ? L - 1 : y - 1;
+    const int zp = (z + 1 == L) ? 0 : z + 1, zm = (z == 0) ? L - 1 : z - 1;
+    const int64_t row = (int64_t)z * L;
+    const uint32_t sw = __ldg(mine + i * W);
+    const uint32_t jbits = __ldg(jbs + i);
+    const uint32_t f0 = sw ^ __ldg(oth + ((row + y) * Lh + xe) * W) ^ jmask(jbits, 0);
+    const uint32_t f1 = sw ^ __ldg(oth + ((row + yp) * Lh + xh) * W) ^ jmask(jbits, 1);
+    const uint32_t f2 = sw ^ __ldg(oth + (((int64_t)zp * L + y) * Lh + xh) * W) ^ jmask(jbits, 2);
+    const uint32_t f3 = sw ^ __ldg(oth + ((row + y) * Lh + xo) * W) ^ jmask(jbits, 3);
+    const uint32_t f4 = sw ^ __ldg(oth + ((row + ym) * Lh + xh) * W) ^ jmask(jbits, 4);
+    const uint32_t f5 = sw ^ __ldg(oth + (((int64_t)zm * L + y) * Lh + xh) * W) ^ jmask(jbits, 5);
+    /* bit-sliced sum of six bits: c = b0 + 2 b1 + 4 b2 */
+    const uint32_t sa = f0 ^ f1 ^ f2, ca = (f0 & f1) | (f2 & (f0 ^ f1));
+    const uint32_t sb = f3 ^ f4 ^ f5, cb = (f3 & f4) | (f5 & (f3 ^ f4));
+    const uint32_t b0 = sa ^ sb, c0 = sa & sb;
+    const uint32_t b1 = ca ^ cb ^ c0, b2 = (ca & cb) | (c0 & (ca ^ cb));
+    acc += __popc(warp_transpose32(b0, lane)) + 2u * __popc(warp_transpose32(b1, lane)) +
+           4u * __popc(warp_transpose32(b2, lane));
+  }
+  atomicAdd(unsat + (int64_t)s * g.nr + w * 32 + lane, acc);
+}
+
+/* Demon energy per replica: blockIdx.y = (plane pi = p*nc + ic)*W + w. */
+__global__ void __launch_bounds__(TPB)
+k_demon_energy(const micsa_geo g, const uint32_t *__restrict__ d0, const uint32_t *__restrict__ d1,
+               unsigned long long *__restrict__ dem) {
+  const int s = blockIdx.z, lane = threadIdx.x & 31;
+  const int w = blockIdx.y % g.W, pi = blockIdx.y / g.W;
+  const int64_t P = g.P, off = ((int64_t)s * 2 * g.nc + pi) * P * g.W + w;
+  unsigned long long acc = 0;
+  const int64_t step = (int64_t)gridDim.x * TPB;
+  for (int64_t base = (int64_t)blockIdx.x * TPB + (threadIdx.x & ~31); base < P; base += step) {
+    const int64_t i = base + lane;
+    const uint32_t a = __ldcs(d0 + off + i * g.W), b = __ldcs(d1 + off + i * g.W);
+    acc += __popc(warp_transpose32(a, lane)) + 2u * __popc(warp_transpose32(b, lane));
+  }
+  atomicAdd(dem + (int64_t)s * g.nr + w * 32 + lane, acc);
+}
+
+/* Overlap and C4 of the replica pairs (2k, 2k+1): with t = s(x) ^ s(x'),
+ * bit 2k of t ^ (t >> 1) is d_x xor d_x', d = a xor b the pair difference.
+ * blockIdx.y = axis*nd + dist (dist 0 also yields q via x' = x and the
+ * second pass below), blockIdx.z = s*W + w.  Sites in natural order. */
+__global__ void __launch_bounds__(TPB)
+k_overlap(const micsa_geo g, const uint32_t *__restrict__ spin, unsigned long long *__restrict__ qd,
+          unsigned long long *__restrict__ c4d) {
+  const int nd = g.L / 2 + 1;
+  const int axis = blockIdx.y / nd, dist = blockIdx.y % nd;
+  const int s = blockIdx.z / g.W, w = blockIdx.z % g.W, lane = threadIdx.x & 31;
+  const int L = g.L, Lh = g.Lh, W = g.W;
+  const int64_t P = g.P, V = 2 * P;
+  const uint32_t *sp = spin + (int64_t)(s * 2) * P * W + w;
+  unsigned long long acc = 0, accq = 0;
+  const bool want_q = (axis == 0 && dist == 0);
+  const int64_t step = (int64_t)gridDim.x * TPB;
+  for (int64_t base = (int64_t)blockIdx.x * TPB + (threadIdx.x & ~31); base < V; base += step) {
+    const int64_t n = base + lane; /* V is a multiple of 32 */
+    const int x = (int)(n % L);
+    const int64_t q = n / L;
+    const int y = (int)(q % L), z = (int)(q / L);
+    int x2 = x, y2 = y, z2 = z;
+    if (axis == 0) { x2 += dist; if (x2 >= L) x2 -= L; }
+    else if (axis == 1) { y2 += dist; if (y2 >= L) y2 -= L; }
+    else { z2 += dist; if (z2 >= L) z2 -= L; }
+    const uint32_t s1 = __ldg(sp + ((int64_t)((x + y + z) & 1) * P + ((int64_t)z * L + y) * Lh + (x >> 1)) * W);
+    const uint32_t s2 = __ldg(sp + ((int64_t)((x2 + y2 + z2) & 1) * P + ((int64_t)z2 * L + y2) * Lh + (x2 >> 1)) * W);
+    const uint32_t t = s1 ^ s2;
+    acc += __popc(warp_transpose32(t ^ (t >> 1), lane));
+    if (want_q) accq += __popc(warp_transpose32(s1 ^ (s1 >> 1), lane));
+  }
+  if (!(lane & 1)) {
+    const int k = w * 16 + (lane >> 1);
+    atomicAdd(c4d + (((int64_t)s * (g.nr / 2) + k) * 3 + axis) * nd + dist, acc);
+    if (want_q) atomicAdd(qd + (int64_t)s * (g.nr / 2) + k, accq);
+  }
+}
+
+inline int blocks_for(int64_t n, int per_block) {
+  int64_t b = (n + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > 2147483647LL) b = 2147483647LL;
+  return (int)b;
+}
+
+} /* namespace */
+
+/* ------------------------------------------------------------ launchers */
+
+template <int VW>
+static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint32_t *spin,
+                            uint32_t *d0, uint32_t *d1, const uint8_t *jb, const int *walk,
+                            const uint32_t *rnd, cudaStream_t st) {
+  const int G = g.W / VW;
+  dim3 grid(blocks_for((int64_t)g.L * g.Lh * G, TPB), g.L, g.ns);
+  if (micsa)
+    k_sweep<VW, true><<<grid, TPB, 0, st>>>(g, p, ic, G, spin, d0, d1, jb, walk, rnd);
+  else
+    k_sweep<VW, false><<<grid, TPB, 0, st>>>(g, p, ic, G, spin, d0, d1, jb, walk, rnd);
+  return cudaGetLastError();
+}
+
+static cudaError_t sweep_any(const micsa_geo &g, int p, int ic, bool micsa, uint32_t *spin,
+                             uint32_t *d0, uint32_t *d1, const uint8_t *jb, const int *walk,
+                             const uint32_t *rnd, cudaStream_t st) {
+  if (g.W % 4 == 0) return sweep_vw<4>(g, p, ic, micsa, spin, d0, d1, jb, walk, rnd, st);
+  if (g.W % 2 == 0) return sweep_vw<2>(g, p, ic, micsa, spin, d0, d1, jb, walk, rnd, st);
+  return sweep_vw<1>(g, p, ic, micsa, spin, d0, d1, jb, walk, rnd, st);
+}
+
+cudaError_t micsa_launch_sweep_micsa(const micsa_geo &g, int p, int ic, uint32_t *spin,
+                                     uint32_t *d0, uint32_t *d1, const uint8_t *jb,
+                                     const int *walk, cudaStream_t st) {
+  return sweep_any(g, p, ic, true, spin, d0, d1, jb, walk, nullptr, st);
+}
+
+cudaError_t micsa_launch_sweep_metropolis(const micsa_geo &g, int p, uint32_t *spin,
+                                          const uint8_t *jb, const uint32_t *rnd,
+                                          cudaStream_t st) {
+  return sweep_any(g, p, 0, false, spin, nullptr, nullptr, jb, nullptr, rnd, st);
+}
+
+cudaError_t micsa_launch_gen_rnd(const micsa_geo &g, int p, const uint32_t *te,
+                                 const uint32_t *keys, const uint8_t *lut, uint32_t *rnd,
+                                 cudaStream_t st) {
+  k_gen_rnd<<<blocks_for(g.H * g.nr, TPB), TPB, 0, st>>>(g, p, te, keys, lut, rnd);
+  return cudaGetLastError();
+}
+
+cudaError_t micsa_launch_walk_advance(const micsa_geo &g, int *walk, cudaStream_t st) {
+  k_walk_advance<<<1, 64, 0, st>>>(walk, g.ns, g.L / 2);
+  return cudaGetLastError();
+}
+
+cudaError_t micsa_launch_from_ref(const micsa_geo &g, int p, int ic, int k, const uint64_t *ref,
+                                  uint32_t *dst, cudaStream_t st) {
+  k_from_ref<<<blocks_for(g.H * g.W, TPB / 32), TPB, 0, st>>>(g, p, ic, k, ref, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t micsa_launch_to_ref(const micsa_geo &g, int p, int ic, const int *walk, int sample,
+                                const uint32_t *src, uint64_t *ref, cudaStream_t st) {
+  k_to_ref<<<blocks_for(g.H * g.W, TPB / 32), TPB, 0, st>>>(g, p, ic, walk, sample, src, ref);
+  return cudaGetLastError();
+}
+
+static int measure_blocks(int64_t sites, int64_t slices) {
+  /* enough blocks to fill the GPU, never more than one per 32-site chunk */
+  int64_t want = (4 * 152 + slices - 1) / slices;
+  int64_t maxb = (sites + TPB - 1) / TPB;
+  if (want > maxb) want = maxb;
+  return want < 1 ? 1 : (int)want;
+}
+
+cudaError_t micsa_launch_energy(const micsa_geo &g, const uint32_t *spin, const uint8_t *jb,
+                                unsigned long long *unsat, cudaStream_t st) {
+  dim3 grid(measure_blocks(g.P, (int64_t)g.W * g.ns), g.W, g.ns);
+  k_energy<<<grid, TPB, 0, st>>>(g, spin, jb, unsat);
+  return cudaGetLastError();
+}
+
+cudaError_t micsa_launch_demon_energy(const micsa_geo &g, const uint32_t *d0, const uint32_t *d1,
+                                      unsigned long long *dem, cudaStream_t st) {
+  dim3 grid(measure_blocks(g.P, (int64_t)2 * g.nc * g.W * g.ns), 2 * g.nc * g.W, g.ns);
+  k_demon_energy<<<grid, TPB, 0, st>>>(g, d0, d1, dem);
+  return cudaGetLastError();
+}
+
+cudaError_t micsa_launch_overlap(const micsa_geo &g, const uint32_t *spin, unsigned long long *qd,
+                                 unsigned long long *c4d, cudaStream_t st) {
+  const int nd = g.L / 2 + 1;
+  dim3 grid(measure_blocks(2 * g.P, (int64_t)3 * nd * g.W * g.ns), 3 * nd, g.ns * g.W);
+  k_overlap<<<grid, TPB, 0, st>>>(g, spin, qd, c4d);
+  return cudaGetLastError();
+}

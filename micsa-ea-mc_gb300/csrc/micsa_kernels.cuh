@@ -1,0 +1,73 @@
+/*
+ * Device layout and kernel launchers of libmicsa.
+ *
+ * Device layout (one sample s; all arrays 32-bit words):
+ *   colour     p = (x + y + z) & 1; a colour holds P = L*L*L/2 sites
+ *   site index i = (z*L + y)*Lh + (x >> 1),  Lh = L/2
+ *   replica    r lives in word r/32, bit r%32; W = nr/32 words per site
+ *   spin       spin[((s*2 + p)*P + i)*W + w]
+ *   demons     d0/d1[(((s*2 + p)*nc + ic)*P + i)*W + w]   (D = d0 + 2*d1)
+ *   couplings  jb[(s*2 + p)*P + i]: bit d = coupling of the bond from the
+ *              site in direction d = +x,+y,+z,-x,-y,-z
+ *   walk       walk[s] = k: demon plane (p, ic) of sample s is stored
+ *              translated; the demon of site x sits at x - sgn*2k*e_axis,
+ *              axis = ic%3, sgn = +1 when (p == 0) == (ic < 3), else -1.
+ * The reference's demon walk (main.cu:1084-1193) moves, per iteration, the
+ * colour-0 demons of plane ic by +2 e_ic and the colour-1 demons by -2 e_ic
+ * (e_3..e_5 = -e_0..-e_2), so keeping k instead of moving data is exact.
+ */
+#ifndef MICSA_KERNELS_CUH
+#define MICSA_KERNELS_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+struct micsa_geo {
+  int L, Lh, W, nc, ns, nr;
+  int64_t P;  /* sites per colour */
+  int64_t H;  /* reference words per colour, (L/4)^3/2 */
+};
+
+/* flag = 1 half-sweep of colour p on demon plane ic, all samples */
+cudaError_t micsa_launch_sweep_micsa(const micsa_geo &g, int p, int ic,
+                                     uint32_t *spin, uint32_t *d0, uint32_t *d1,
+                                     const uint8_t *jb, const int *walk,
+                                     cudaStream_t st);
+/* flag = 0 half-sweep of colour p with random words rnd[(k*P + i)*W + w] */
+cudaError_t micsa_launch_sweep_metropolis(const micsa_geo &g, int p,
+                                          uint32_t *spin, const uint8_t *jb,
+                                          const uint32_t *rnd, cudaStream_t st);
+/* Philox4x32-10 heat-bath words for colour p: te[r*4+k], keys[r] on device,
+ * lut = 4096-byte table on device */
+cudaError_t micsa_launch_gen_rnd(const micsa_geo &g, int p, const uint32_t *te,
+                                 const uint32_t *keys, const uint8_t *lut,
+                                 uint32_t *rnd, cudaStream_t st);
+/* walk[s] = (walk[s] + 1) mod L/2 for all samples */
+cudaError_t micsa_launch_walk_advance(const micsa_geo &g, int *walk,
+                                      cudaStream_t st);
+
+/* reference-layout words ref[h*nr + r] (one colour, one sample/plane) ->
+ * device words dst (colour p base of that plane), demon translation k
+ * (0 for spins) applied with plane index ic (ignored when k == 0) */
+cudaError_t micsa_launch_from_ref(const micsa_geo &g, int p, int ic, int k,
+                                  const uint64_t *ref, uint32_t *dst,
+                                  cudaStream_t st);
+cudaError_t micsa_launch_to_ref(const micsa_geo &g, int p, int ic,
+                                const int *walk, int sample,
+                                const uint32_t *src, uint64_t *ref,
+                                cudaStream_t st);
+
+/* measurement accumulators (unsigned long long, zeroed by the caller):
+ *   unsat[s*nr + r], dem[s*nr + r], qd[s*(nr/2) + k],
+ *   c4d[((s*(nr/2) + k)*3 + axis)*(L/2+1) + d] */
+cudaError_t micsa_launch_energy(const micsa_geo &g, const uint32_t *spin,
+                                const uint8_t *jb, unsigned long long *unsat,
+                                cudaStream_t st);
+cudaError_t micsa_launch_demon_energy(const micsa_geo &g, const uint32_t *d0,
+                                      const uint32_t *d1,
+                                      unsigned long long *dem, cudaStream_t st);
+cudaError_t micsa_launch_overlap(const micsa_geo &g, const uint32_t *spin,
+                                 unsigned long long *qd, unsigned long long *c4d,
+                                 cudaStream_t st);
+
+#endif

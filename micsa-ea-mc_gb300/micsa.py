@@ -1,0 +1,360 @@
+"""ctypes binding of libmicsa (include/micsa.h) for tests and benchmarks.
+
+The product is the C ABI; this module only loads the in-tree shared library
+and wraps numpy arrays.  Loading fails loudly when the library has not been
+built -- there is no fallback implementation.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libmicsa.so")
+DRIVER_PATH = os.path.join(PKG, "bin", "micsa_run")
+
+MICSA_OK = 0
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE", 5: "ERR_UNSUPPORTED"}
+
+# symbols declared in include/micsa.h (checked by the CPU test suite)
+ABI_SYMBOLS = [
+    "micsa_create", "micsa_destroy", "micsa_last_error", "micsa_footprint_bytes",
+    "micsa_set_lut", "micsa_upload_couplings", "micsa_upload_spins", "micsa_upload_demons",
+    "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
+    "micsa_download_demons", "micsa_synchronize", "micsa_kernel_launches", "micsa_stream",
+]
+
+_lib = None
+
+
+class MicsaError(RuntimeError):
+    pass
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int), ("L", C.c_int), ("nr", C.c_int),
+                ("nsamples", C.c_int), ("nc", C.c_int)]
+
+
+class PRC(C.Structure):
+    """micsa_prc_t: the reference's s_aleatorio_HQ_64bits (2080 bytes)."""
+    _fields_ = [("ira", C.c_uint64 * 256), ("pr", C.c_uint64), ("zseed", C.c_uint64),
+                ("out", C.c_uint64), ("ip", C.c_ubyte), ("ip1", C.c_ubyte), ("ip2", C.c_ubyte),
+                ("ip3", C.c_ubyte), ("pad", C.c_ubyte * 4)]
+
+
+class Xoshiro(C.Structure):
+    """micsa_xoshiro_t: the reference's s_xoshiro256pp (48 bytes)."""
+    _fields_ = [("s", C.c_uint64 * 4), ("t", C.c_uint64), ("out", C.c_uint64)]
+
+
+def _ptr(a, ctype):
+    if a is None:
+        return None
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def lib():
+    """Load libmicsa.so (build it first with micsa-ea-mc_gb300/build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise MicsaError("libmicsa.so is not built (%s); run build()" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    u64p, u32p, i32p, i64p, u8p = (C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_uint8))
+    sig = {
+        "micsa_create": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
+        "micsa_destroy": (C.c_int, [C.c_void_p]),
+        "micsa_last_error": (C.c_char_p, [C.c_void_p]),
+        "micsa_footprint_bytes": (C.c_int64, [C.POINTER(Config)]),
+        "micsa_set_lut": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+        "micsa_upload_couplings": (C.c_int, [C.c_void_p, C.c_int, u64p]),
+        "micsa_upload_spins": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
+        "micsa_upload_demons": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
+        "micsa_monte_carlo": (C.c_int, [C.c_void_p, C.c_int, u32p, u32p]),
+        "micsa_iterate": (C.c_int, [C.c_void_p, C.c_int64]),
+        "micsa_measure": (C.c_int, [C.c_void_p, i32p, u64p, i64p, i64p]),
+        "micsa_download_spins": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
+        "micsa_download_demons": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
+        "micsa_synchronize": (C.c_int, [C.c_void_p]),
+        "micsa_kernel_launches": (C.c_int64, [C.c_void_p]),
+        "micsa_stream": (C.c_void_p, [C.c_void_p]),
+        # host side (micsa-ea-mc_gb300/host/micsa_host.h)
+        "micsa_check_seed": (C.c_uint64, [C.c_uint64]),
+        "micsa_init_cpu_generators": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), u32p, C.c_uint64]),
+        "micsa_init_rand_hq": (None, [C.POINTER(PRC), C.c_uint64]),
+        "micsa_seeds_from_one": (None, [u64p, u64p, C.c_int]),
+        "micsa_half_words": (C.c_int64, [C.c_int]),
+        "micsa_pack_spins": (None, [C.c_int, C.c_int, u8p, u64p, u64p]),
+        "micsa_unpack_spins": (None, [C.c_int, C.c_int, u64p, u64p, u8p]),
+        "micsa_pack_couplings": (None, [C.c_int, u8p, u8p, u8p, u64p]),
+        "micsa_init_spins": (C.c_int, [C.POINTER(PRC), C.c_int, C.c_int, C.c_int, i32p, C.c_int, u8p]),
+        "micsa_init_couplings_janus": (C.c_int, [C.c_uint64, C.c_int, u8p, u8p, u8p]),
+        "micsa_thresholds": (None, [C.c_double, u64p]),
+        "micsa_draw_demons_all": (C.c_int, [C.POINTER(PRC), C.POINTER(Xoshiro), u64p, C.c_int,
+                                            C.c_int, C.c_int, u64p, u64p, C.c_int]),
+        "micsa_fill_bits": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), C.c_int, C.c_uint64,
+                                   C.c_int, C.c_uint32, u32p]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(ctx, rc, what):
+    if rc != MICSA_OK:
+        msg = lib().micsa_last_error(ctx) if ctx else b""
+        raise MicsaError("%s failed: %s %s" % (what, STATUS.get(rc, rc), (msg or b"").decode()))
+
+
+class Context:
+    """One libmicsa context (device state of nsamples x nr replicas)."""
+
+    def __init__(self, L, nr, nsamples=1, nc=6, device=0):
+        self.L, self.nr, self.ns, self.nc = L, nr, nsamples, nc
+        self.H = (L // 4) ** 3 // 2
+        self.cfg = Config(device, L, nr, nsamples, nc)
+        h = C.c_void_p()
+        rc = lib().micsa_create(C.byref(self.cfg), C.byref(h))
+        if rc != MICSA_OK:
+            raise MicsaError("micsa_create failed: %s" % STATUS.get(rc, rc))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().micsa_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_lut(self, lut):
+        b = np.ascontiguousarray(np.frombuffer(bytes(lut), dtype=np.uint8))
+        check(self.h, lib().micsa_set_lut(self.h, b.ctypes.data_as(C.c_void_p), b.size), "set_lut")
+
+    def upload_couplings(self, s, J):
+        J = np.ascontiguousarray(J, dtype=np.uint64)
+        check(self.h, lib().micsa_upload_couplings(self.h, s, _ptr(J, C.c_uint64)), "upload_couplings")
+
+    def upload_spins(self, s, even, odd):
+        e = np.ascontiguousarray(even, dtype=np.uint64)
+        o = np.ascontiguousarray(odd, dtype=np.uint64)
+        check(self.h, lib().micsa_upload_spins(self.h, s, _ptr(e, C.c_uint64), _ptr(o, C.c_uint64)),
+              "upload_spins")
+
+    def upload_demons(self, s, w0, w1):
+        a = np.ascontiguousarray(w0, dtype=np.uint64)
+        b = np.ascontiguousarray(w1, dtype=np.uint64)
+        check(self.h, lib().micsa_upload_demons(self.h, s, _ptr(a, C.c_uint64), _ptr(b, C.c_uint64)),
+              "upload_demons")
+
+    def monte_carlo(self, flag, te=None, keys=None):
+        t = None if te is None else np.ascontiguousarray(te, dtype=np.uint32)
+        k = None if keys is None else np.ascontiguousarray(keys, dtype=np.uint32)
+        check(self.h, lib().micsa_monte_carlo(self.h, flag, _ptr(t, C.c_uint32), _ptr(k, C.c_uint32)),
+              "monte_carlo")
+
+    def iterate(self, n):
+        check(self.h, lib().micsa_iterate(self.h, n), "iterate")
+
+    def synchronize(self):
+        check(self.h, lib().micsa_synchronize(self.h), "synchronize")
+
+    def measure(self, spin=True, demon=True, overlap=False):
+        ns, nr, nd = self.ns, self.nr, self.L // 2 + 1
+        es = np.zeros(ns * nr, np.int32) if spin else None
+        ed = np.zeros(ns * nr, np.uint64) if demon else None
+        q = np.zeros(ns * (nr // 2), np.int64) if overlap else None
+        c4 = np.zeros(ns * (nr // 2) * 3 * nd, np.int64) if overlap else None
+        check(self.h, lib().micsa_measure(self.h, _ptr(es, C.c_int32), _ptr(ed, C.c_uint64),
+                                          _ptr(q, C.c_int64), _ptr(c4, C.c_int64)), "measure")
+        out = {}
+        if spin:
+            out["e_spin"] = es.reshape(ns, nr)
+        if demon:
+            out["e_demon"] = ed.reshape(ns, nr)
+        if overlap:
+            out["q"] = q.reshape(ns, nr // 2)
+            out["c4"] = c4.reshape(ns, nr // 2, 3, nd)
+        return out
+
+    def download_spins(self, s):
+        e = np.zeros(self.H * self.nr, np.uint64)
+        o = np.zeros(self.H * self.nr, np.uint64)
+        check(self.h, lib().micsa_download_spins(self.h, s, _ptr(e, C.c_uint64), _ptr(o, C.c_uint64)),
+              "download_spins")
+        return e, o
+
+    def download_demons(self, s):
+        n = 2 * self.H * self.nc * self.nr
+        a = np.zeros(n, np.uint64)
+        b = np.zeros(n, np.uint64)
+        check(self.h, lib().micsa_download_demons(self.h, s, _ptr(a, C.c_uint64), _ptr(b, C.c_uint64)),
+              "download_demons")
+        return a, b
+
+    def kernel_launches(self):
+        return lib().micsa_kernel_launches(self.h)
+
+    def stream(self):
+        return lib().micsa_stream(self.h)
+
+
+# ------------------------------------------------------------------ host side
+class Streams:
+    """Host generator state of one run (the reference's globals of ini.c)."""
+
+
+def check_seed(seed):
+    return lib().micsa_check_seed(seed)
+
+
+def seeds_from_one(seed, n):
+    s = C.c_uint64(seed)
+    out = np.zeros(n, np.uint64)
+    lib().micsa_seeds_from_one(C.byref(s), _ptr(out, C.c_uint64), n)
+    return s.value, out
+
+
+def init_cpu_generators(seed):
+    p, x, k = PRC(), Xoshiro(), C.c_uint32()
+    lib().micsa_init_cpu_generators(C.byref(p), C.byref(x), C.byref(k), seed)
+    return p, x, k.value
+
+
+def init_rand_hq(seed):
+    p = PRC()
+    lib().micsa_init_rand_hq(C.byref(p), seed)
+    return p
+
+
+def thresholds(beta):
+    t = np.zeros(3, np.uint64)
+    lib().micsa_thresholds(beta, _ptr(t, C.c_uint64))
+    return t
+
+
+def couplings_janus(seed, L):
+    V = L ** 3
+    Jx, Jy, Jz = (np.zeros(V, np.uint8) for _ in range(3))
+    count = lib().micsa_init_couplings_janus(seed, L, _ptr(Jx, C.c_uint8), _ptr(Jy, C.c_uint8),
+                                             _ptr(Jz, C.c_uint8))
+    return Jx, Jy, Jz, count
+
+
+def pack_couplings(L, Jx, Jy, Jz):
+    H = (L // 4) ** 3 // 2
+    J = np.zeros(12 * H, np.uint64)
+    lib().micsa_pack_couplings(L, _ptr(Jx, C.c_uint8), _ptr(Jy, C.c_uint8), _ptr(Jz, C.c_uint8),
+                               _ptr(J, C.c_uint64))
+    return J
+
+
+def pack_spins(L, nr, uu):
+    H = (L // 4) ** 3 // 2
+    e = np.zeros(H * nr, np.uint64)
+    o = np.zeros(H * nr, np.uint64)
+    uu = np.ascontiguousarray(uu, dtype=np.uint8)
+    lib().micsa_pack_spins(L, nr, _ptr(uu, C.c_uint8), _ptr(e, C.c_uint64), _ptr(o, C.c_uint64))
+    return e, o
+
+
+def unpack_spins(L, nr, even, odd):
+    uu = np.zeros(nr * L ** 3, np.uint8)
+    e = np.ascontiguousarray(even, dtype=np.uint64)
+    o = np.ascontiguousarray(odd, dtype=np.uint64)
+    lib().micsa_unpack_spins(L, nr, _ptr(e, C.c_uint64), _ptr(o, C.c_uint64), _ptr(uu, C.c_uint8))
+    return uu
+
+
+class HostModel:
+    """The reference's host initialisation (ini.c Init) for one run:
+    seeds, Metropolis streams, spins, couplings, demon streams."""
+
+    MAXNSAMPLES = 2
+
+    def __init__(self, L, nr, nc, seed_J, seed_u, seed_MC, list_samples=(0,), beta=0.9090909090909,
+                 nthreads=8):
+        Lb = lib()
+        self.L, self.nr, self.nc, self.beta = L, nr, nc, beta
+        self.nbits = len(list_samples)
+        self.list_samples = list(list_samples)
+        self.V = L ** 3
+        self.H = (L // 4) ** 3 // 2
+        self.nthreads = nthreads
+        # get_seeds (io.c:794-799): the Janus build uses one fixed coupling seed
+        self.seed_J, _ = seeds_from_one(seed_J, self.MAXNSAMPLES)
+        self.seeds_J = [9164166177945067407] * self.nbits
+        # Init_Random (ini.c:34-60)
+        self.seed_u = check_seed(seed_u)
+        self.seed_MC = [check_seed(s) for s in seed_MC]
+        self.random_u = init_rand_hq(self.seed_u)
+        self.prc = (PRC * nr)()
+        self.xo = (Xoshiro * nr)()
+        self.keys = np.zeros(nr, np.uint32)
+        for r in range(nr):
+            k = C.c_uint32()
+            Lb.micsa_init_cpu_generators(C.byref(self.prc[r]), C.byref(self.xo[r]), C.byref(k),
+                                         self.seed_MC[r])
+            self.keys[r] = k.value
+        self.seed_u, self.seeds_C = seeds_from_one(self.seed_u, self.MAXNSAMPLES * nr)
+        self.prc_C, self.xo_C = [], []
+        for b in range(self.nbits):
+            pa, xa = (PRC * nr)(), (Xoshiro * nr)()
+            for r in range(nr):
+                k = C.c_uint32()
+                Lb.micsa_init_cpu_generators(C.byref(pa[r]), C.byref(xa[r]), C.byref(k),
+                                             int(self.seeds_C[b * nr + r]))
+            self.prc_C.append(pa)
+            self.xo_C.append(xa)
+        # Init_u (ini.c:275-299)
+        self.uu = np.zeros(self.nbits * nr * self.V, np.uint8)
+        ls = np.array(self.list_samples + [0] * (self.MAXNSAMPLES + 1 - self.nbits), np.int32)
+        rc = Lb.micsa_init_spins(C.byref(self.random_u), L, nr, self.MAXNSAMPLES,
+                                 _ptr(ls, C.c_int32), self.nbits, _ptr(self.uu, C.c_uint8))
+        if rc:
+            raise MicsaError("Problems generating spins")
+        self.uu = self.uu.reshape(self.nbits, nr, self.V)
+        self.spins = [pack_spins(L, nr, self.uu[b]) for b in range(self.nbits)]
+        # Init_J / packing_J (ini.c:425-578)
+        self.Jsite, self.J = [], []
+        for b in range(self.nbits):
+            Jx, Jy, Jz, count = couplings_janus(self.seeds_J[b], L)
+            self.Jsite.append((Jx, Jy, Jz, count))
+            self.J.append(pack_couplings(L, Jx, Jy, Jz))
+        self.thr = thresholds(beta)
+
+    def draw_demons(self, b):
+        """InitWalkers (ini.c:712-781) for sample b: CPUwalker0/1 words."""
+        n = 2 * self.H * self.nc * self.nr
+        w0 = np.zeros(n, np.uint64)
+        w1 = np.zeros(n, np.uint64)
+        rc = lib().micsa_draw_demons_all(self.prc_C[b], self.xo_C[b], _ptr(self.thr, C.c_uint64),
+                                         self.L, self.nr, self.nc, _ptr(w0, C.c_uint64),
+                                         _ptr(w1, C.c_uint64), self.nthreads)
+        if rc:
+            raise MicsaError("demon draw failed")
+        return w0, w1
+
+    def fill_bits(self, it, parity, jobid):
+        """_fill_bits (fill_bits.h:47-68): Philox counters of one call."""
+        te = np.zeros(4 * self.nr, np.uint32)
+        lib().micsa_fill_bits(self.prc, self.xo, self.nr, it, parity, jobid, _ptr(te, C.c_uint32))
+        return te
