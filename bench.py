@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""bench.py -- micSA sweep throughput on GB300, in spin-flip attempts per ps.
+
+Workload (one GPU): the plain micSA run at L=160, 2 disorder samples x 64
+replicas, nc = 6 demons per site.  One step = one reference iteration
+(Monte_Carlo flag=1, PROGRAM/src/main.cu:254-305): 6 x (even, odd)
+half-sweeps plus the demon walk, on both samples, i.e.
+V * 64 * 2 * 6 = 3.15e9 spin-flip attempts (timing.c:20-23 counts the same).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl micsa|reference]
+
+--gpus N > 1 is launched by torchrun (one process per GPU): every rank runs
+its own independent copy of the workload (the path has no exchange step;
+replicas only) and the value is the total over ranks divided by the slowest
+rank's time.  --impl reference times the CPU restatement of the reference's
+algorithm (oracle/) on the host cores, on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "micsa-ea-mc_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "spin-flips/ps at L=160"
+UNIT = "spin-flip attempts/ps"
+SEEDS = dict(seed_J=20260101, seed_u=1729, seed_MC0=0x5EED0000)
+BETA = 0.90909090909090
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="micsa", choices=["micsa", "reference"])
+    # smaller shapes for profiling captures (the headline is the default)
+    ap.add_argument("--L", type=int, default=160)
+    ap.add_argument("--nr", type=int, default=64)
+    ap.add_argument("--nsamples", type=int, default=2)
+    ap.add_argument("--nc", type=int, default=6)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class Dist:
+    """torch.distributed plumbing: barrier and max over ranks (nccl on GPUs,
+    gloo where there is none)."""
+
+    def __init__(self, backend=None):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            import torch
+            if backend is None:
+                backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend)
+            self.pg = dist
+            self.backend = backend
+
+    def barrier(self):
+        if self.pg:
+            if self.backend == "nccl":
+                import torch
+                self.pg.barrier(device_ids=[self.local])
+            else:
+                self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        dev = "cuda:%d" % self.local if self.backend == "nccl" else "cpu"
+        t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons while running."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, device):
+        self.device, self.proc, self.out = device, None, None
+
+    def start(self):
+        try:
+            self.out = open(os.devnull, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=self.out, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            text, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            text, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        for line in text.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(self.NAMES, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes_per_attempt(nr):
+    # per 64 attempts (one colour site-word x one replica word, one
+    # half-sweep): own spin r+w 16 B, other-colour spin 8 B, demon r+w 32 B,
+    # couplings 48/nr B (shared by the replicas)
+    return (56.0 + 48.0 / nr) / 64.0
+
+
+def traffic_per_launch(L, nr, ns):
+    """DRAM bytes of one half-sweep launch from the committed ncu summary
+    (profiles/k_sweep_*.md, line 'traffic_bytes_per_launch L nr ns: N'),
+    scaled by the sites processed when only a smaller capture exists."""
+    import glob
+    import re
+    best = None
+    for f in glob.glob(os.path.join(ROOT, "profiles", "*.md")):
+        for m in re.finditer(r"traffic_bytes_per_launch L=(\d+) nr=(\d+) ns=(\d+): (\d+)",
+                             open(f).read()):
+            cl, cn, cs, b = (int(x) for x in m.groups())
+            if (cl, cn, cs) == (L, nr, ns):
+                return float(b), "ncu capture of this shape"
+            if cn == nr:
+                best = (float(b) * (L ** 3 * ns) / (cl ** 3 * cs),
+                        "ncu capture at L=%d ns=%d scaled by sites" % (cl, cs))
+    return best if best else (None, None)
+
+
+def run_micsa(a, dist):
+    import torch
+    import micsa
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    L, nr, ns, nc = a.L, a.nr, a.nsamples, a.nc
+    hm = micsa.HostModel(L, nr, nc, SEEDS["seed_J"], SEEDS["seed_u"],
+                         [SEEDS["seed_MC0"] + r for r in range(nr)], list(range(ns)), beta=BETA,
+                         nthreads=os.cpu_count() or 8)
+    demons = [hm.draw_demons(b) for b in range(ns)]
+    ctx = micsa.Context(L, nr, ns, nc, device=dev)
+    for b in range(ns):
+        ctx.upload_couplings(b, hm.J[b])
+        ctx.upload_spins(b, *hm.spins[b])
+        ctx.upload_demons(b, *demons[b])
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    attempts = float(L ** 3) * nr * ns * nc
+    # ---- device-resident throughput: one graph replay per step
+    for _ in range(a.warmup):
+        ctx.iterate(1)
+    ctx.synchronize()
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    clocks.start()
+    l0 = ctx.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        ctx.iterate(1)
+    e1.record(stream)
+    e1.synchronize()
+    ctx.synchronize()
+    launches = ctx.kernel_launches() - l0
+    torch.cuda.synchronize()
+    dist.barrier()
+    ck = clocks.stop()
+    ms = dist.max(e0.elapsed_time(e1) / a.steps)
+    value = attempts * dist.world / (ms * 1e9)
+    # ---- dominant kernel: mean half-sweep launch time, CUDA events
+    sweep_ms, iter_ms = ctx.profile(max(3, min(10, a.steps)))
+    bpa = algorithmic_bytes_per_attempt(nr)
+    per_launch = attempts / (2 * nc) * bpa
+    achieved = per_launch / (sweep_ms * 1e-3) / 1e9
+    peak, kind = peaks()
+    traffic, tnote = traffic_per_launch(L, nr, ns)
+    roof = {"bound": "hbm", "kernel": "k_sweep<2,true> (micSA half-sweep)",
+            "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": kind,
+            "algorithmic_bytes_per_launch": int(per_launch),
+            "launch_ms": round(sweep_ms, 5), "iteration_ms_profiled": round(iter_ms, 5),
+            "traffic": traffic, "traffic_source": tnote}
+    # ---- end to end through the C ABI with host buffers: every step uploads
+    # the demon refresh set from pinned memory (refresh_walkers), runs the
+    # iteration and reads the energies back (Measure_Energy_Spins + demons)
+    e2e = None
+    if not a.no_e2e:
+        pinned = []
+        for b in range(ns):
+            pair = []
+            for w in demons[b]:
+                t = torch.empty(w.size, dtype=torch.int64, pin_memory=True)
+                arr = t.numpy().view(np.uint64)
+                arr[:] = w
+                pair.append((t, arr))
+            pinned.append(pair)
+        h2d = sum(p[1].nbytes for pair in pinned for p in pair)
+        d2h = ns * nr * (4 + 8)
+        for _ in range(max(1, a.warmup)):
+            for b in range(ns):
+                ctx.upload_demons(b, pinned[b][0][1], pinned[b][1][1])
+            ctx.iterate(1)
+            ctx.measure(spin=True, demon=True)
+        ke = max(3, a.steps // 2)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            for b in range(ns):
+                ctx.upload_demons(b, pinned[b][0][1], pinned[b][1][1])
+            ctx.iterate(1)
+            ctx.measure(spin=True, demon=True)
+        te = dist.max((time.perf_counter() - t0) / ke)
+        e2e = {"value": round(attempts * dist.world / (te * 1e12), 4), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": round(te * 1e3, 4), "steps": ke,
+               "step": "upload demon refresh set (pinned host) + 1 iteration + energy readback"}
+    ctx.close()
+    return dict(value=value, ms=ms, roof=roof, clocks=ck, e2e=e2e, launches=launches,
+                attempts=attempts)
+
+
+def cpu_state(L, nr, ns, nc, seed=7):
+    """Seeded random reference-layout state for the CPU arms (same shapes)."""
+    import micsa
+    rng = np.random.default_rng(seed)
+    H = (L // 4) ** 3 // 2
+    out = []
+    for _ in range(ns):
+        J = micsa.pack_couplings(L, *(rng.integers(0, 2, size=L ** 3, dtype=np.uint8)
+                                      for _ in range(3)))
+        e = rng.integers(0, 2 ** 63, size=H * nr, dtype=np.uint64)
+        o = rng.integers(0, 2 ** 63, size=H * nr, dtype=np.uint64)
+        w0 = rng.integers(0, 2 ** 63, size=2 * H * nc * nr, dtype=np.uint64)
+        w1 = rng.integers(0, 2 ** 63, size=2 * H * nc * nr, dtype=np.uint64) & w0
+        out.append([J, e, o, w0, w1])
+    return out
+
+
+def cpu_iterations(L, nr, nc, states, n, threads):
+    """n iterations of the oracle (the reference algorithm on its own layout,
+    every replica range on its own thread); returns attempts/ps."""
+    import oracle
+    t0 = time.perf_counter()
+    for _ in range(n):
+        for J, e, o, w0, w1 in states:
+            oracle.micsa_iteration(L, nr, nc, J, e, o, w0, w1, threads)
+    dt = time.perf_counter() - t0
+    return float(L ** 3) * nr * nc * len(states) * n / (dt * 1e12), dt
+
+
+def cpu_baseline(a, budget_s=10.0):
+    """Bounded sample: oracle iterations of ONE sample of the workload on all
+    host cores until ~budget_s of wall time."""
+    threads = os.cpu_count() or 1
+    st = cpu_state(a.L, a.nr, 1, a.nc)
+    v, dt = cpu_iterations(a.L, a.nr, a.nc, st, 1, threads)
+    n = max(1, int(budget_s / max(dt, 1e-3)))
+    v, dt = cpu_iterations(a.L, a.nr, a.nc, st, n, threads)
+    return {"value": round(v, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d oracle iteration(s) of 1 of %d samples (L=%d, %d replicas, nc=%d), %.1f s"
+                      % (n, a.nsamples, a.L, a.nr, a.nc, dt)}
+
+
+def run_reference(a):
+    """CPU restatement of the reference (oracle/) on the host cores: each
+    step is one full iteration of the workload (both samples)."""
+    threads = os.cpu_count() or 1
+    st = cpu_state(a.L, a.nr, a.nsamples, a.nc)
+    cpu_iterations(a.L, a.nr, a.nc, st, a.warmup, threads)
+    v, dt = cpu_iterations(a.L, a.nr, a.nc, st, a.steps, threads)
+    return v, dt / a.steps * 1e3, threads
+
+
+def config(a):
+    return {"workload": "plain micSA, L=%d periodic +-J lattice, %d samples x %d replicas "
+                        "(uint32 words), nc=%d demons/site; step = one iteration = %d half-sweeps "
+                        "+ demon walk" % (a.L, a.nsamples, a.nr, a.nc, 2 * a.nc),
+            "L": a.L, "replicas": a.nr, "samples": a.nsamples, "nc": a.nc,
+            "beta": BETA, "l2": "inputs larger than L2: each step streams %.0f MB of demon planes"
+                                % (a.nsamples * 2 * a.nc * 2 * a.L ** 3 / 2 * a.nr / 8 / 1e6),
+            "parallelism": "replicas (an independent lattice per GPU)"}
+
+
+def main():
+    a = parse()
+    dist = Dist()
+    line = {"metric": METRIC, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
+            "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic: seeded reference initialisation (Janus couplings, uniform spins, "
+                    "heat-bath demons at beta=0.909)", "config": config(a)}
+    if a.impl == "reference":
+        if dist.rank != 0:
+            dist.close()
+            return
+        v, ms, threads = run_reference(a)
+        line.update({"impl": "reference", "value": round(v, 6), "ms_per_step": round(ms, 3),
+                     "n_gpus": dist.world, "dtype": "u64",
+                     "data": "synthetic: seeded random reference-layout state",
+                     "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": threads,
+                                      "kind": "port",
+                                      "sample": "full workload step (both samples), CPU oracle"},
+                     "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0,
+                             "d2h_bytes_per_step": 0}})
+        print(json.dumps(line))
+        dist.close()
+        return
+    r = run_micsa(a, dist)
+    line.update({"value": round(r["value"], 4), "ms_per_step": round(r["ms"], 4),
+                 "roofline": r["roof"], "e2e": r["e2e"], "gpu_launches": r["launches"],
+                 "clocks": r["clocks"]})
+    if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(a)
+    if dist.rank == 0:
+        print(json.dumps(line))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

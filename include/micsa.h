@@ -107,6 +107,12 @@ int micsa_download_spins(micsa_ctx *ctx, int sample, uint64_t *even,
 int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0,
                           uint64_t *w1);
 
+/* Run n microcanonical iterations with CUDA events around every launch and
+ * report the mean device time of one half-sweep launch and of one whole
+ * iteration, in milliseconds (the per-kernel view of measure_time,
+ * timing.c:3-33).  Advances the state like micsa_iterate. */
+int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration_ms);
+
 /* Wait for all work issued on the context (cudaDeviceSynchronize,
  * main.cu:144,149) and report any asynchronous error. */
 int micsa_synchronize(micsa_ctx *ctx);

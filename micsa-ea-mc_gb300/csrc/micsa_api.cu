@@ -234,6 +234,17 @@ void *micsa_stream(micsa_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr;
 int micsa_set_lut(micsa_ctx *ctx, const void *lut, size_t bytes) {
   if (!ctx || !lut) return fail(ctx, MICSA_ERR_ARG, "null argument");
   if (bytes != 4096) return fail(ctx, MICSA_ERR_ARG, "LUT must be 4096 bytes, got %zu", bytes);
+  /* thresholds non-decreasing, prebisection ranges ordered */
+  const uint32_t *w = (const uint32_t *)lut;
+  for (int i = 1; i < 256; i++) {
+    const uint64_t a = ((uint64_t)w[2 * i - 2] << 32) | w[2 * i - 1];
+    const uint64_t b = ((uint64_t)w[2 * i] << 32) | w[2 * i + 1];
+    if (b < a) return fail(ctx, MICSA_ERR_ARG, "LUT thresholds decrease at %d", i);
+  }
+  const uint16_t *pre = (const uint16_t *)((const uint8_t *)lut + 2048);
+  for (int i = 0; i < 1024; i++)
+    if ((pre[i] & 255) > (pre[i] >> 8))
+      return fail(ctx, MICSA_ERR_ARG, "LUT prebisection entry %d has min > max", i);
   int rc = set_device(ctx);
   if (rc) return rc;
   MICSA_CK(cudaMemcpyAsync(ctx->lut, lut, 4096, cudaMemcpyHostToDevice, ctx->stream));
@@ -439,6 +450,44 @@ int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0, uint64_t *w1
     MICSA_CK(cudaMemcpyAsync(dst[k], ctx->stage, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
   }
   MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  return MICSA_OK;
+}
+
+int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration_ms) {
+  if (!ctx || n < 1) return fail(ctx, MICSA_ERR_ARG, "bad argument");
+  int rc = set_device(ctx);
+  if (rc || (rc = ready_for_sweeps(ctx, 1))) return rc;
+  const micsa_geo &g = ctx->g;
+  const int per = 2 * g.nc;
+  std::vector<cudaEvent_t> ev((size_t)(n * (per + 1) + 1));
+  for (auto &e : ev) MICSA_CK(cudaEventCreate(&e));
+  size_t k = 0;
+  MICSA_CK(cudaEventRecord(ev[k++], ctx->stream));
+  for (int64_t it = 0; it < n; it++) {
+    for (int ic = 0; ic < g.nc; ic++)
+      for (int p = 0; p < 2; p++) {
+        MICSA_CK(micsa_launch_sweep_micsa(g, p, ic, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
+                                          ctx->walk, ctx->stream));
+        MICSA_CK(cudaEventRecord(ev[k++], ctx->stream));
+      }
+    MICSA_CK(micsa_launch_walk_advance(g, ctx->walk, ctx->stream));
+    MICSA_CK(cudaEventRecord(ev[k++], ctx->stream));
+  }
+  ctx->launches += n * (per + 1);
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  double sweep = 0, total = 0;
+  k = 0;
+  for (int64_t it = 0; it < n; it++) {
+    for (int j = 0; j <= per; j++, k++) {
+      float ms = 0;
+      MICSA_CK(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+      if (j < per) sweep += ms;
+      total += ms;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (sweep_ms) *sweep_ms = sweep / (double)(n * per);
+  if (iteration_ms) *iteration_ms = total / (double)n;
   return MICSA_OK;
 }
 

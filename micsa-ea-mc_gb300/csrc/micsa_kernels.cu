@@ -244,7 +244,8 @@ __device__ __forceinline__ uint32_t lut_bisect(uint32_t hi, uint32_t lo, const u
     a = e & 255u;
     b = e >> 8;
   }
-  while (b - a > 1) {
+  /* a <= b (checked when the LUT is uploaded): at most 8 halvings */
+  for (int step = 0; step < 8 && b - a > 1; step++) {
     const uint32_t mid = (a + b) >> 1;
     if (MICSA_BELOW(mid)) b = mid; else a = mid;
   }

@@ -21,7 +21,8 @@ ABI_SYMBOLS = [
     "micsa_create", "micsa_destroy", "micsa_last_error", "micsa_footprint_bytes",
     "micsa_set_lut", "micsa_upload_couplings", "micsa_upload_spins", "micsa_upload_demons",
     "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
-    "micsa_download_demons", "micsa_synchronize", "micsa_kernel_launches", "micsa_stream",
+    "micsa_download_demons", "micsa_profile", "micsa_synchronize", "micsa_kernel_launches",
+    "micsa_stream",
 ]
 
 _lib = None
@@ -81,6 +82,8 @@ def lib():
         "micsa_measure": (C.c_int, [C.c_void_p, i32p, u64p, i64p, i64p]),
         "micsa_download_spins": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
         "micsa_download_demons": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
+        "micsa_profile": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double)]),
         "micsa_synchronize": (C.c_int, [C.c_void_p]),
         "micsa_kernel_launches": (C.c_int64, [C.c_void_p]),
         "micsa_stream": (C.c_void_p, [C.c_void_p]),
@@ -209,6 +212,12 @@ class Context:
         check(self.h, lib().micsa_download_demons(self.h, s, _ptr(a, C.c_uint64), _ptr(b, C.c_uint64)),
               "download_demons")
         return a, b
+
+    def profile(self, n):
+        """(mean half-sweep launch ms, mean iteration ms) over n iterations."""
+        a, b = C.c_double(), C.c_double()
+        check(self.h, lib().micsa_profile(self.h, n, C.byref(a), C.byref(b)), "profile")
+        return a.value, b.value
 
     def kernel_launches(self):
         return lib().micsa_kernel_launches(self.h)

@@ -95,6 +95,29 @@ static void free_tables(tables_t *t) {
   free(t->rot);
 }
 
+/* ISI demon algebra (main.cu:1037-1074): returns the flip mask and
+ * updates D = D0 + 2*D1 in place. */
+static uint64_t isi(uint64_t j1, uint64_t j2, uint64_t j3, uint64_t j4,
+                    uint64_t *D0p, uint64_t *D1p) {
+  uint64_t D0 = *D0p, D1 = *D1p;
+  uint64_t x13 = j1 ^ j3, x24 = j2 ^ j4;
+  uint64_t sub = (x24 & (~j1 & ~j3)) | (~j2 & ~j4);
+  uint64_t s0 = ~x13;
+  uint64_t s1 = ~x24 & (x13 | (s0 & ~(j1 ^ j2)));
+  s1 = (~sub & s1) | (sub & (s1 ^ s0));
+  uint64_t n0 = D0 ^ s0, k1 = D0 & s0, k2 = D1 ^ s1, n1 = k1 ^ k2, k3 = D1 & s1;
+  uint64_t carry = (k3 | (k2 & k1)) ^ sub;
+  uint64_t flip = ~carry;
+  *D0p = (flip & n0) | (~flip & D0);
+  *D1p = (flip & n1) | (~flip & D1);
+  return flip;
+}
+
+uint64_t oracle_isi_word(uint64_t j1, uint64_t j2, uint64_t j3, uint64_t j4,
+                         uint64_t *D0, uint64_t *D1) {
+  return isi(j1, j2, j3, j4, D0, D1);
+}
+
 /* Body of d_oneMCstepBN_multisample (main.cu:899-1078) for one word. */
 static void sweep_word(const tables_t *t, int nr, int p, int64_t h, int r,
                        const uint64_t *J, uint64_t *mine, const uint64_t *other,
@@ -130,17 +153,7 @@ static void sweep_word(const tables_t *t, int nr, int p, int64_t h, int r,
     flip = (j1 & j3 & id1) | ((j24 | id2) & (j1 | j3 | id1)) | ((j2 & j4) | (j24 & id2));
   } else {
     /* microcanonical demon update, ISI algebra (main.cu:1037-1074) */
-    uint64_t D0 = d0[h * nr + r], D1 = d1[h * nr + r];
-    uint64_t x13 = j1 ^ j3, x24 = j2 ^ j4;
-    uint64_t sub = (x24 & (~j1 & ~j3)) | (~j2 & ~j4);
-    uint64_t s0 = ~x13;
-    uint64_t s1 = ~x24 & (x13 | (s0 & ~(j1 ^ j2)));
-    s1 = (~sub & s1) | (sub & (s1 ^ s0));
-    uint64_t n0 = D0 ^ s0, k1 = D0 & s0, k2 = D1 ^ s1, n1 = k1 ^ k2, k3 = D1 & s1;
-    uint64_t carry = (k3 | (k2 & k1)) ^ sub;
-    flip = ~carry;
-    d0[h * nr + r] = (flip & n0) | (~flip & D0);
-    d1[h * nr + r] = (flip & n1) | (~flip & D1);
+    flip = isi(j1, j2, j3, j4, &d0[h * nr + r], &d1[h * nr + r]);
   }
   mine[h * nr + r] = s ^ flip;
 }

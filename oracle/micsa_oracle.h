@@ -67,6 +67,10 @@ void oracle_energy(int L, int nr, const uint64_t *J, const uint64_t *even,
 void oracle_demon_energy(int L, int nr, int nc, const uint64_t *w0,
                          const uint64_t *w1, uint64_t *ener);
 
+/* the ISI demon algebra on one word (main.cu:1037-1074) */
+uint64_t oracle_isi_word(uint64_t j1, uint64_t j2, uint64_t j3, uint64_t j4,
+                         uint64_t *D0, uint64_t *D1);
+
 /* ---- plain scalar rendering on unpacked spins uu[r*V + x+L*y+L*L*z] ---- */
 /* accept/demon rule per site: returns new demon, sets *flip */
 int oracle_scalar_rule(int unsatisfied, int demon, int *flip);

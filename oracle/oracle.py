@@ -70,6 +70,8 @@ def lib():
             "oracle_energy": (None, [C.c_int, C.c_int, u64p, u64p, u64p, i32p]),
             "oracle_demon_energy": (None, [C.c_int, C.c_int, C.c_int, u64p, u64p, u64p]),
             "oracle_scalar_rule": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int)]),
+            "oracle_isi_word": (C.c_uint64, [C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64,
+                                             u64p, u64p]),
             "oracle_overlap_c4": (None, [C.c_int, C.c_int, u8p, i64p, i64p]),
             "oracle_scalar_energy": (C.c_int32, [C.c_int, u8p, u8p, u8p, u8p]),
         }
@@ -145,6 +147,12 @@ def scalar_rule(u, d):
     f = C.c_int()
     nd = lib().oracle_scalar_rule(u, d, C.byref(f))
     return nd, f.value
+
+
+def isi_word(j1, j2, j3, j4, d0, d1):
+    a, b = C.c_uint64(d0), C.c_uint64(d1)
+    f = lib().oracle_isi_word(j1, j2, j3, j4, C.byref(a), C.byref(b))
+    return f, a.value, b.value
 
 
 def scalar_energy(L, u, Jx, Jy, Jz):

@@ -62,6 +62,10 @@ def write_inputs(d, cfg):
         f.write(lut_bytes())
     argv = [str(cfg.get("isample", 0)), str(cfg["nbits"]), "beta.in", "input.in", "lut.bin",
             "times.in", "0"]
+    if cfg.get("list_samples"):
+        with open(os.path.join(d, "samples.in"), "w") as f:
+            f.write("\n".join(str(s) for s in cfg["list_samples"]) + "\n")
+        argv += ["0", "samples.in"]
     return argv
 
 
@@ -153,19 +157,91 @@ def data_record(cfg, now, seed_J, seed_u, seed_MC, flag=1):
             + struct.pack("<%dQ" % (2 + cfg["nr"]), seed_J, seed_u, *seed_MC))
 
 
-def oracle_run(cfg, nthreads=8, on_state=None):
-    """The reference main loop with product host init and oracle kernels."""
-    import oracle
+class OracleEngine:
+    """Sweeps on the CPU oracle, state in the reference layouts."""
+
+    def __init__(self, cfg, hm, lut, nthreads=8):
+        import oracle
+        self.o, self.cfg, self.nthreads, self.lut = oracle, cfg, nthreads, lut
+        self.even = [hm.spins[b][0].copy() for b in range(cfg["nbits"])]
+        self.odd = [hm.spins[b][1].copy() for b in range(cfg["nbits"])]
+        self.J = hm.J
+        self.w0 = [None] * cfg["nbits"]
+        self.w1 = [None] * cfg["nbits"]
+
+    def metropolis(self, te0, te1, keys):
+        c = self.cfg
+        for b in range(c["nbits"]):
+            self.o.metropolis_iteration(c["L"], c["nr"], self.J[b], self.even[b], self.odd[b],
+                                        te0, te1, keys, self.lut)
+
+    def set_demons(self, b, w0, w1):
+        self.w0[b], self.w1[b] = w0.copy(), w1.copy()
+
+    def iterate(self, n):
+        c = self.cfg
+        for _ in range(n):
+            for b in range(c["nbits"]):
+                self.o.micsa_iteration(c["L"], c["nr"], c["nc"], self.J[b], self.even[b],
+                                       self.odd[b], self.w0[b], self.w1[b], self.nthreads)
+
+    def state(self, b):
+        return self.even[b], self.odd[b], self.w0[b], self.w1[b]
+
+    def energies(self, b):
+        c = self.cfg
+        return (self.o.energy(c["L"], c["nr"], self.J[b], self.even[b], self.odd[b]),
+                self.o.demon_energy(c["L"], c["nr"], c["nc"], self.w0[b], self.w1[b]))
+
+
+class GpuEngine:
+    """Sweeps on the GPU through the C ABI (libmicsa)."""
+
+    def __init__(self, cfg, hm, lut, device=0):
+        c = cfg
+        self.cfg = cfg
+        self.ctx = micsa.Context(c["L"], c["nr"], c["nbits"], c["nc"], device)
+        self.ctx.set_lut(lut)
+        for b in range(c["nbits"]):
+            self.ctx.upload_couplings(b, hm.J[b])
+            self.ctx.upload_spins(b, hm.spins[b][0], hm.spins[b][1])
+        self._meas = None
+
+    def metropolis(self, te0, te1, keys):
+        self.ctx.monte_carlo(0, np.concatenate([te0, te1]), keys)
+
+    def set_demons(self, b, w0, w1):
+        self.ctx.upload_demons(b, w0, w1)
+
+    def iterate(self, n):
+        self.ctx.iterate(n)
+        self._meas = None
+
+    def state(self, b):
+        e, o = self.ctx.download_spins(b)
+        w0, w1 = self.ctx.download_demons(b)
+        return e, o, w0, w1
+
+    def energies(self, b):
+        if self._meas is None:
+            self._meas = self.ctx.measure(spin=True, demon=True)
+        return self._meas["e_spin"][b], self._meas["e_demon"][b]
+
+    def close(self):
+        self.ctx.close()
+
+
+def model_run(cfg, engine="oracle", nthreads=8, on_state=None, device=0):
+    """The reference main loop (main.cu:121-180) with product host init and
+    sweeps on `engine` ("oracle" or "gpu"); returns a run summary."""
     L, nr, nc, nbits = cfg["L"], cfg["nr"], cfg["nc"], cfg["nbits"]
     samples = cfg.get("list_samples") or list(range(nbits))
     jobid = cfg.get("isample", 0)
     hm = micsa.HostModel(L, nr, nc, cfg["seed_J"], cfg["seed_u"], seeds_mc(cfg), samples,
                          beta=float(BETA_TEXT), nthreads=nthreads)
     lut = lut_bytes()[8:]
+    eng = OracleEngine(cfg, hm, lut, nthreads) if engine == "oracle" else GpuEngine(cfg, hm, lut, device)
     V = L ** 3
-    even = [hm.spins[b][0].copy() for b in range(nbits)]
-    odd = [hm.spins[b][1].copy() for b in range(nbits)]
-    J = hm.J
     res = {"evol": {str(b): {"E_spins": "", "E_walkers": "", "T_walkers": ""} for b in range(nbits)},
            "seeds_in": {}, "conf_Js": {}, "times": {}, "walkers": {},
            "master_seedJ": "%d\n" % hm.seed_J}
@@ -179,36 +255,38 @@ def oracle_run(cfg, nthreads=8, on_state=None):
     for t in range(cfg["nterm"]):
         te0 = hm.fill_bits(2 * t, 0, jobid)
         te1 = hm.fill_bits(2 * t + 1, 1, jobid)
-        for b in range(nbits):
-            oracle.metropolis_iteration(L, nr, J[b], even[b], odd[b], te0, te1, hm.keys, lut)
-    w0 = [None] * nbits
-    w1 = [None] * nbits
+        eng.metropolis(te0, te1, hm.keys)
     snap = [None] * nbits
-    spin_off, nsb = conf_layout(L, nr)
     times = measured(cfg)
-    it, i = 0, 0
-    prev_t = 0
+    it, i, prev_t = 0, 0, 0
     while it < cfg["maxtime"] and i < len(times):
         if not (it & (it - 1)):
             for b in range(nbits):
-                w0[b], w1[b] = hm.draw_demons(b)
+                w0, w1 = hm.draw_demons(b)
+                eng.set_demons(b, w0, w1)
                 snap[b] = (bytes(hm.prc_C[b]), bytes(hm.xo_C[b]))
-        for b in range(nbits):
-            oracle.micsa_iteration(L, nr, nc, J[b], even[b], odd[b], w0[b], w1[b], nthreads)
-        it += 1
+        # run to the next refresh or measurement
+        nxt, p2 = times[i], 1
+        while p2 <= it:
+            p2 <<= 1
+        nxt = min(nxt, p2, cfg["maxtime"])
         if on_state:
-            on_state(it, even, odd, w0, w1)
+            nxt = it + 1
+        eng.iterate(nxt - it)
+        it = nxt
+        if on_state:
+            on_state(it, eng)
         if it == times[i]:
             for b in range(nbits):
-                e = oracle.energy(L, nr, J[b], even[b], odd[b])
-                ed = oracle.demon_energy(L, nr, nc, w0[b], w1[b])
-                es_m, es_s = _stats([float(-x) / V for x in e], nr)
-                ec_m, ec_s = _stats([float(x) / (float(V) * nc) for x in ed], nr)
+                e, ed = eng.energies(b)
+                even, odd, w0, w1 = eng.state(b)
+                es_m, es_s = _stats([float(-int(x)) / V for x in e], nr)
+                ec_m, ec_s = _stats([float(int(x)) / (float(V) * nc) for x in ed], nr)
                 ev = res["evol"][str(b)]
                 ev["E_spins"] += _evol_line(it, es_m, es_s)
                 ev["E_walkers"] += _evol_line(it, ec_m, ec_s)
                 ev["T_walkers"] += "%d %14.10g \n" % (it, 1.0 / (0.25 * math.log(1.0 + 1.0 / ec_m)))
-                uu = micsa.unpack_spins(L, nr, even[b], odd[b]).reshape(nr, V)
+                uu = micsa.unpack_spins(L, nr, even, odd).reshape(nr, V)
                 spins, confs = [], []
                 drec = data_record(cfg, it, JANUS_SEED, hm.seed_u, hm.seed_MC)
                 for r in range(nr):
@@ -221,13 +299,19 @@ def oracle_run(cfg, nthreads=8, on_state=None):
                     "energies": [int(x) for x in e]}
                 icds = struct.pack("<6IQd", 0, b, nr, nc, L, 0,
                                    int(hm.seeds_C[samples[b]]), float(BETA_TEXT))
-                dem = w0[b].tobytes() + w1[b].tobytes()
+                dem = w0.tobytes() + w1.tobytes()
                 res["walkers"][str(b)] = {"file": sha(icds + snap[b][0] + snap[b][1] + dem),
                                           "demons": sha(dem)}
             prev_t = it
             i += 1
     res["final_time"] = prev_t
+    if hasattr(eng, "close"):
+        eng.close()
     return res
+
+
+def oracle_run(cfg, nthreads=8):
+    return model_run(cfg, "oracle", nthreads)
 
 
 def compare(got, want, what="run"):

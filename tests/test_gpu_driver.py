@@ -1,0 +1,58 @@
+"""micsa_run, the command-line drop-in, against the reference program's own
+outputs: same argv and input files, byte-identical measurement files, seed
+files, conf.<t> records and walkers files."""
+import os
+import shutil
+import tempfile
+
+import pytest
+
+import micsa
+import runs
+from conftest import golden_cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def workdir():
+    d = tempfile.mkdtemp(prefix="micsa_drv_")
+    yield d
+    shutil.rmtree(d, ignore_errors=True)
+
+
+@pytest.mark.parametrize("golden", golden_cases())
+def test_driver_matches_reference_files(golden, workdir):
+    got, out = runs.run_program(micsa.DRIVER_PATH, golden["cfg"], workdir)
+    runs.compare(got, golden, "micsa_run %s" % golden["cfg"])
+    assert "finished at iteration" in out
+
+
+def test_driver_resume_is_bit_exact(workdir):
+    """Stop at an intermediate measurement (maxtime), resume with flag 0 from
+    the conf/walkers checkpoints, and end where an uninterrupted run ends.
+    (A case without thermalisation: the reference re-runs its nterm
+    Metropolis steps on every start, main.cu:124-128, resumed or not; and a
+    resumed run records flag 0 in its conf records.)"""
+    import json
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "L16_NR64_2s_nc6.json")))
+    cfg = dict(g["cfg"])
+    assert cfg["nterm"] == 0
+    runs.run_program(micsa.DRIVER_PATH, dict(cfg, maxtime=16), workdir)
+    got, _ = runs.run_program(micsa.DRIVER_PATH, dict(cfg, flag=0), workdir)
+    for t in ("32", "64", "128"):
+        for b in ("0", "1"):
+            assert got["times"][t][b]["spins"] == g["times"][t][b]["spins"]
+            assert got["times"][t][b]["energies"] == g["times"][t][b]["energies"]
+    assert got["walkers"] == g["walkers"]
+    assert got["evol"] == g["evol"]
+
+
+def test_driver_rejects_bad_input(workdir):
+    import subprocess
+    cfg = dict(L=12, nr=32, nbits=1, nc=6, nterm=0, maxtime=4, times=[1], seed_J=1, seed_u=2,
+               seed_MC0=3)
+    argv = runs.write_inputs(workdir, cfg)
+    p = subprocess.run([micsa.DRIVER_PATH] + argv, cwd=workdir, stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True)
+    assert p.returncode != 0 and "multiple of 8" in p.stdout
