@@ -38,7 +38,7 @@ BETA = 0.90909090909090
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="micsa", choices=["micsa", "reference"])
     # smaller shapes for profiling captures (the headline is the default)

@@ -69,7 +69,7 @@ def build(verbose=False, force=False):
         o = os.path.join(OBJ, os.path.basename(src) + ".o")
         objs.append(o)
         if force or not _newer(o, [s] + hdrs):
-            jobs.append(["gcc", "-O3", "-std=gnu11", "-fPIC", "-Wall", "-Wextra",
+            jobs.append(["gcc", "-O3", "-std=gnu11", "-ffp-contract=off", "-fPIC", "-Wall", "-Wextra",
                          "-Wno-unused-parameter", "-pthread"] + inc + ["-c", s, "-o", o])
     for src in CUDA:
         s = os.path.join(PKG, src)
@@ -89,7 +89,7 @@ def build(verbose=False, force=False):
     drv_src = os.path.join(PKG, "host", "micsa_driver.c")
     drv = os.path.join(BIN, "micsa_run")
     if force or not _newer(drv, [drv_src, lib] + hdrs):
-        _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-pthread"] + inc +
+        _run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-Wall", "-pthread"] + inc +
              [drv_src, "-o", drv, "-L" + LIB, "-lmicsa", "-Wl,-rpath,$ORIGIN/../lib", "-lm"])
     return lib
 

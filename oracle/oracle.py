@@ -27,7 +27,7 @@ def build(force=False):
     if (not force and os.path.exists(LIB)
             and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
         return LIB
-    subprocess.run(["gcc", "-O3", "-std=gnu11", "-fPIC", "-shared", "-pthread", "-Wall",
+    subprocess.run(["gcc", "-O3", "-std=gnu11", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-Wall",
                     src, "-o", LIB], check=True)
     return LIB
 
