@@ -88,6 +88,11 @@ int check_cfg(const micsa_config *c, char *msg, size_t n) {
            MICSA_ERR_ARG;
   if (c->nc < 1 || c->nc > 6)
     return snprintf(msg, n, "nc=%d must be in [1, 6]", c->nc), MICSA_ERR_ARG;
+  /* sweep kernels index one colour plane with 32-bit word offsets */
+  const uint64_t words = (uint64_t)c->L * c->L * c->L / 2 * (uint64_t)(c->nr / 32);
+  if (words >= (1ULL << 32))
+    return snprintf(msg, n, "L=%d with nr=%d exceeds 2^32 words per colour plane", c->L, c->nr),
+           MICSA_ERR_UNSUPPORTED;
   return MICSA_OK;
 }
 

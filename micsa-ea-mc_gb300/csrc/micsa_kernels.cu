@@ -56,6 +56,80 @@ __device__ __forceinline__ void st_stream(uint32_t *p, const uint32_t (&o)[VW]) 
   __stcs(reinterpret_cast<typename vt<VW>::T *>(p), pack(o));
 }
 
+/* L2 residency policies for the sweeps: the spin lattice and the coupling
+ * bytes (re-read by every half-sweep) are kept with evict_last; the demon
+ * planes (touched once per iteration) are streamed with evict_first. */
+__device__ __forceinline__ uint64_t l2_keep() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_stream() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+/* loads/stores with an L2 cache policy: nc = read-only (non-coherent) path,
+ * na = no L1 allocation (data used once) */
+template <int VW> struct hint;
+template <> struct hint<1> {
+  static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[1], uint64_t pol) {
+    asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(o[0]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[1], uint64_t pol) {
+    asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(o[0]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t (&o)[1], uint64_t pol) {
+    asm volatile("ld.global.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
+                 : "=r"(o[0]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void st(uint32_t *a, const uint32_t (&o)[1], uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" :: "l"(a), "r"(o[0]), "l"(pol) : "memory");
+  }
+};
+template <> struct hint<2> {
+  static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[2], uint64_t pol) {
+    asm("ld.global.nc.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
+        : "=r"(o[0]), "=r"(o[1]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[2], uint64_t pol) {
+    asm volatile("ld.global.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
+                 : "=r"(o[0]), "=r"(o[1]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t (&o)[2], uint64_t pol) {
+    asm volatile("ld.global.L1::no_allocate.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
+                 : "=r"(o[0]), "=r"(o[1]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void st(uint32_t *a, const uint32_t (&o)[2], uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.u32 [%0], {%1,%2}, %3;"
+                 :: "l"(a), "r"(o[0]), "r"(o[1]), "l"(pol) : "memory");
+  }
+};
+template <> struct hint<4> {
+  static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[4], uint64_t pol) {
+    asm("ld.global.nc.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+        : "=r"(o[0]), "=r"(o[1]), "=r"(o[2]), "=r"(o[3]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[4], uint64_t pol) {
+    asm volatile("ld.global.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=r"(o[0]), "=r"(o[1]), "=r"(o[2]), "=r"(o[3]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t (&o)[4], uint64_t pol) {
+    asm volatile("ld.global.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=r"(o[0]), "=r"(o[1]), "=r"(o[2]), "=r"(o[3]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void st(uint32_t *a, const uint32_t (&o)[4], uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1,%2,%3,%4}, %5;"
+                 :: "l"(a), "r"(o[0]), "r"(o[1]), "r"(o[2]), "r"(o[3]), "l"(pol) : "memory");
+  }
+};
+__device__ __forceinline__ uint32_t ld_byte_keep(const uint8_t *a, uint64_t pol) {
+  uint32_t v;
+  asm("ld.global.nc.L2::cache_hint.u8 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
+
 /* ------------------------------------------------------------ geometry */
 struct site_xyz { int x, y, z; };
 
@@ -135,64 +209,84 @@ __device__ __forceinline__ uint32_t metropolis_flip(uint32_t j1, uint32_t j2, ui
   return (j1 & j3 & id1) | ((j24 | id2) & (j1 | j3 | id1)) | ((j2 & j4) | (j24 & id2));
 }
 
-/* One thread = one site of colour p and VW consecutive replica words of it.
- * blockIdx.z = sample, blockIdx.y = z plane, x covers (y, x/2, word group). */
+/* One thread = one site of colour p and VW replica words of it (group grp of
+ * G = W/VW).  Block = (TX sites along x/2) x (TY rows); TX divides L/2, so no
+ * thread index needs a division.  grid = (L/2/TX, ytiles*ns*G, L): sample,
+ * row tile and word group come from the block index, z from blockIdx.z.
+ * In-plane offsets are 32-bit (P*W < 2^32 is checked at creation). */
 template <int VW, bool MICSA>
 __global__ void __launch_bounds__(TPB)
-k_sweep(const micsa_geo g, const int p, const int ic, const int G,
+k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
         uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
         uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
         const int *__restrict__ walk, const uint32_t *__restrict__ rnd) {
-  const int s = blockIdx.z;
-  const int z = blockIdx.y;
-  const int L = g.L, Lh = g.Lh, W = g.W;
-  const int64_t j = (int64_t)blockIdx.x * TPB + threadIdx.x;
-  if (j >= (int64_t)L * Lh * G) return;
-  const int grp = (int)(j % G);
-  const int ps = (int)(j / G);
-  const int y = ps / Lh;
-  const int xh = ps - y * Lh;
-  const int64_t P = g.P;
-
-  const int rowoff = (y + z + p) & 1; /* x = 2*xh + rowoff */
-  int xe = xh + rowoff;
-  if (xe == Lh) xe = 0;
-  int xo = xh + rowoff - 1;
-  if (xo < 0) xo = Lh - 1;
-  const int yp = (y + 1 == L) ? 0 : y + 1, ym = (y == 0) ? L - 1 : y - 1;
-  const int zp = (z + 1 == L) ? 0 : z + 1, zm = (z == 0) ? L - 1 : z - 1;
-  const int64_t row = (int64_t)z * L;
-  const int64_t i = (row + y) * Lh + xh;
-
-  uint32_t *mine = spin + (int64_t)(s * 2 + p) * P * W + grp * VW;
-  const uint32_t *oth = spin + (int64_t)(s * 2 + (p ^ 1)) * P * W + grp * VW;
+  const uint32_t L = g.L, Lh = g.Lh, W = g.W;
+  const uint32_t by = blockIdx.y;
+  const uint32_t tile = by % ytiles, sg = by / ytiles; /* block-uniform */
+  const uint32_t s = sg / G, grp = sg % G;
+  const uint32_t y = tile * blockDim.y + threadIdx.y;
+  if (y >= L) return;
+  const uint32_t xh = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t z = blockIdx.z;
+  const uint32_t plane = L * Lh;
+  const uint32_t i = (z * L + y) * Lh + xh;
+  const uint32_t rowoff = (y + z + p) & 1; /* x = 2*xh + rowoff */
+  /* other-colour neighbours: +x is at x/2 + rowoff, -x at x/2 + rowoff - 1 */
+  const uint32_t iE = rowoff ? (xh + 1 == Lh ? i + 1 - Lh : i + 1) : i;
+  const uint32_t iO = rowoff ? i : (xh == 0 ? i + Lh - 1 : i - 1);
+  const uint32_t iN = (y + 1 == L) ? i - (L - 1) * Lh : i + Lh;
+  const uint32_t iS = (y == 0) ? i + (L - 1) * Lh : i - Lh;
+  const uint32_t iU = (z + 1 == L) ? i - (L - 1) * plane : i + plane;
+  const uint32_t iD = (z == 0) ? i + (L - 1) * plane : i - plane;
+  const size_t P = (size_t)g.P;
+  uint32_t *mine = spin + (size_t)(s * 2 + p) * P * W + grp * VW;
+  const uint32_t *oth = spin + (size_t)(s * 2 + (p ^ 1)) * P * W + grp * VW;
+  const uint64_t keep = l2_keep(), strm = l2_stream();
 
   uint32_t sv[VW], nE[VW], nN[VW], nU[VW], nO[VW], nS[VW], nD[VW];
-  ld_rw<VW>(mine + i * W, sv);
-  ld_ro<VW>(oth + ((row + y) * Lh + xe) * W, nE);
-  ld_ro<VW>(oth + ((row + yp) * Lh + xh) * W, nN);
-  ld_ro<VW>(oth + (((int64_t)zp * L + y) * Lh + xh) * W, nU);
-  ld_ro<VW>(oth + ((row + y) * Lh + xo) * W, nO);
-  ld_ro<VW>(oth + ((row + ym) * Lh + xh) * W, nS);
-  ld_ro<VW>(oth + (((int64_t)zm * L + y) * Lh + xh) * W, nD);
-  const uint32_t jbits = __ldg(jb + (int64_t)(s * 2 + p) * P + i);
+  hint<VW>::ld(mine + i * W, sv, keep);
+  hint<VW>::ld_nc(oth + iE * W, nE, keep);
+  hint<VW>::ld_nc(oth + iN * W, nN, keep);
+  hint<VW>::ld_nc(oth + iU * W, nU, keep);
+  hint<VW>::ld_nc(oth + iO * W, nO, keep);
+  hint<VW>::ld_nc(oth + iS * W, nS, keep);
+  hint<VW>::ld_nc(oth + iD * W, nD, keep);
+  const uint32_t jbits = ld_byte_keep(jb + (size_t)(s * 2 + p) * P + i, keep);
   const uint32_t m0 = jmask(jbits, 0), m1 = jmask(jbits, 1), m2 = jmask(jbits, 2);
   const uint32_t m3 = jmask(jbits, 3), m4 = jmask(jbits, 4), m5 = jmask(jbits, 5);
 
   uint32_t a0[VW], a1[VW], a2[VW];
   uint32_t *q0 = nullptr, *q1 = nullptr;
   if (MICSA) {
-    const int64_t slot = demon_slot(g, p, ic, walk[s], 2 * xh + rowoff, y, z);
-    const int64_t base = ((int64_t)(s * 2 + p) * g.nc + ic) * P * W + grp * VW;
-    q0 = d0 + base + slot * W;
-    q1 = d1 + base + slot * W;
-    ld_stream<VW>(q0, a0);
-    ld_stream<VW>(q1, a1);
+    /* demon of this site after k walks: stored 2k sites back along the
+     * plane's axis (see micsa_kernels.cuh) */
+    const int k = walk[s];
+    const int sh = ((p == 0) == (ic < 3)) ? k : -k; /* in units of 2 sites */
+    const int axis = ic < 3 ? ic : ic - 3;
+    uint32_t slot = i;
+    if (axis == 0) {
+      int xd = (int)xh - sh;
+      xd += xd < 0 ? (int)Lh : (xd >= (int)Lh ? -(int)Lh : 0);
+      slot = i - xh + (uint32_t)xd;
+    } else if (axis == 1) {
+      int yd = (int)y - 2 * sh;
+      yd += yd < 0 ? (int)L : (yd >= (int)L ? -(int)L : 0);
+      slot = i + (uint32_t)((yd - (int)y) * (int)Lh);
+    } else {
+      int zd = (int)z - 2 * sh;
+      zd += zd < 0 ? (int)L : (zd >= (int)L ? -(int)L : 0);
+      slot = (uint32_t)((int)i + (zd - (int)z) * (int)plane);
+    }
+    const size_t base = ((size_t)(s * 2 + p) * g.nc + ic) * P * W + grp * VW;
+    q0 = d0 + base + (size_t)slot * W;
+    q1 = d1 + base + (size_t)slot * W;
+    hint<VW>::ld_na(q0, a0, strm);
+    hint<VW>::ld_na(q1, a1, strm);
   } else {
-    const uint32_t *rb = rnd + i * W + grp * VW;
-    ld_stream<VW>(rb, a0);
-    ld_stream<VW>(rb + P * W, a1);
-    ld_stream<VW>(rb + 2 * P * W, a2);
+    const uint32_t *rb = rnd + (size_t)i * W + grp * VW;
+    hint<VW>::ld_na(rb, a0, strm);
+    hint<VW>::ld_na(rb + P * W, a1, strm);
+    hint<VW>::ld_na(rb + 2 * P * W, a2, strm);
   }
 
 #pragma unroll
@@ -209,10 +303,10 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int G,
       flip = metropolis_flip(j1, j2, j3, j4, a0[w], a1[w], a2[w]);
     sv[w] = sw ^ flip;
   }
-  st_rw<VW>(mine + i * W, sv);
+  hint<VW>::st(mine + i * W, sv, keep);
   if (MICSA) {
-    st_stream<VW>(q0, a0);
-    st_stream<VW>(q1, a1);
+    hint<VW>::st(q0, a0, strm);
+    hint<VW>::st(q1, a1, strm);
   }
 }
 
@@ -481,11 +575,18 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
                             uint32_t *d0, uint32_t *d1, const uint8_t *jb, const int *walk,
                             const uint32_t *rnd, cudaStream_t st) {
   const int G = g.W / VW;
-  dim3 grid(blocks_for((int64_t)g.L * g.Lh * G, TPB), g.L, g.ns);
+  /* TX sites along x/2 per block row: the largest power of two <= 32 that
+   * divides L/2 (L/2 is a multiple of 4) */
+  int tx = 32;
+  while (g.Lh % tx) tx >>= 1;
+  const int ty = TPB / tx;
+  const int ytiles = (g.L + ty - 1) / ty;
+  dim3 block(tx, ty);
+  dim3 grid(g.Lh / tx, ytiles * g.ns * G, g.L);
   if (micsa)
-    k_sweep<VW, true><<<grid, TPB, 0, st>>>(g, p, ic, G, spin, d0, d1, jb, walk, rnd);
+    k_sweep<VW, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, spin, d0, d1, jb, walk, rnd);
   else
-    k_sweep<VW, false><<<grid, TPB, 0, st>>>(g, p, ic, G, spin, d0, d1, jb, walk, rnd);
+    k_sweep<VW, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, spin, d0, d1, jb, walk, rnd);
   return cudaGetLastError();
 }
 
