@@ -226,6 +226,7 @@ def run_micsa(a, dist):
             "frac": round(achieved / peak, 4), "peak_kind": kind,
             "algorithmic_bytes_per_launch": int(per_launch),
             "launch_ms": round(sweep_ms, 5), "iteration_ms_profiled": round(iter_ms, 5),
+            "autotune": ctx.tuning(),
             "traffic": traffic, "traffic_source": tnote}
     # ---- end to end through the C ABI with host buffers: every step uploads
     # the demon refresh set from pinned memory (refresh_walkers), runs the

@@ -113,6 +113,11 @@ int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0,
  * timing.c:3-33).  Advances the state like micsa_iterate. */
 int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration_ms);
 
+/* Text line describing the launch shape the context's autotuner chose at
+ * creation: "zc=<z planes per thread> <candidate>:<ms per half-sweep> ...".
+ * The reference has fixed launch geometry (calculate_blocks, ini.c:580-602). */
+int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n);
+
 /* Wait for all work issued on the context (cudaDeviceSynchronize,
  * main.cu:144,149) and report any asynchronous error. */
 int micsa_synchronize(micsa_ctx *ctx);

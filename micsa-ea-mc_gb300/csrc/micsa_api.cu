@@ -33,6 +33,9 @@ struct micsa_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int64_t launches = 0;
+  int ntune = 0;           /* slab-depth candidates timed at creation */
+  int tune_zc[8] = {0};
+  double tune_ms[8] = {0};
   char err[512] = {0};
 };
 
@@ -134,6 +137,47 @@ int ready_for_sweeps(micsa_ctx *ctx, int need_demons) {
   return MICSA_OK;
 }
 
+/* Slab-depth autotuner: time a (colour 0, colour 1) pair of micSA
+ * half-sweeps for every z-chunk length that divides L, on the freshly zeroed
+ * buffers, keep the fastest, then zero the buffers again.  Results do not
+ * depend on the choice (each site is updated by exactly one thread either
+ * way); only the speed does. */
+int autotune(micsa_ctx *ctx) {
+  micsa_geo &g = ctx->g;
+  int cand[8];
+  const int n = micsa_sweep_zc_candidates(g.L, cand, 8);
+  cudaEvent_t e0, e1;
+  MICSA_CK(cudaEventCreate(&e0));
+  MICSA_CK(cudaEventCreate(&e1));
+  double best = 1e30;
+  int best_zc = cand[n - 1];
+  const int reps = 4;
+  for (int c = 0; c < n; c++) {
+    g.zc = cand[c];
+    for (int rep = -1; rep < reps; rep++) { /* rep -1: warm-up */
+      if (rep == 0) MICSA_CK(cudaEventRecord(e0, ctx->stream));
+      for (int p = 0; p < 2; p++)
+        MICSA_CK(micsa_launch_sweep_micsa(g, p, 0, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
+                                          ctx->walk, ctx->stream));
+    }
+    MICSA_CK(cudaEventRecord(e1, ctx->stream));
+    MICSA_CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    MICSA_CK(cudaEventElapsedTime(&ms, e0, e1));
+    ctx->tune_zc[c] = cand[c];
+    ctx->tune_ms[c] = ms / (2.0 * reps);
+    if (ctx->tune_ms[c] < best) {
+      best = ctx->tune_ms[c];
+      best_zc = cand[c];
+    }
+  }
+  ctx->ntune = n;
+  g.zc = best_zc;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return MICSA_OK;
+}
+
 int enqueue_micsa_iteration(micsa_ctx *ctx) {
   const micsa_geo &g = ctx->g;
   for (int ic = 0; ic < g.nc; ic++)
@@ -177,6 +221,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.ns = cfg->nsamples;
   g.nr = cfg->nr;
   g.P = s.P;
+  g.zc = 0;
   g.H = s.H;
   ctx->stage_words = (size_t)s.stage_w;
   ctx->acc_words = (size_t)s.acc_w;
@@ -211,7 +256,25 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem0, 0, 4 * s.dem_w, ctx->stream));
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem1, 0, 4 * s.dem_w, ctx->stream));
   MICSA_CK_CREATE(cudaStreamSynchronize(ctx->stream));
+  if ((rc = autotune(ctx)) != MICSA_OK) {
+    fprintf(stderr, "micsa_create: autotune: %s\n", ctx->err);
+    micsa_destroy(ctx);
+    *out = nullptr;
+    return rc;
+  }
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->spin, 0, 4 * s.spin_w, ctx->stream));
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem0, 0, 4 * s.dem_w, ctx->stream));
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem1, 0, 4 * s.dem_w, ctx->stream));
+  MICSA_CK_CREATE(cudaStreamSynchronize(ctx->stream));
 #undef MICSA_CK_CREATE
+  return MICSA_OK;
+}
+
+int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
+  if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
+  int k = snprintf(buf, n, "zc=%d", ctx->g.zc);
+  for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
+    k += snprintf(buf + k, n - (size_t)k, " %d:%.5fms", ctx->tune_zc[c], ctx->tune_ms[c]);
   return MICSA_OK;
 }
 

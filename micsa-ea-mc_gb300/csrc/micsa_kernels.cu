@@ -15,47 +15,7 @@ namespace {
 constexpr int TPB = 256;
 constexpr unsigned FULL = 0xffffffffu;
 
-/* ---------------------------------------------------------------- vectors */
-template <int VW> struct vt;
-template <> struct vt<1> { typedef uint32_t T; };
-template <> struct vt<2> { typedef uint2 T; };
-template <> struct vt<4> { typedef uint4 T; };
-
-__device__ __forceinline__ void unpack(uint32_t t, uint32_t (&o)[1]) { o[0] = t; }
-__device__ __forceinline__ void unpack(uint2 t, uint32_t (&o)[2]) { o[0] = t.x; o[1] = t.y; }
-__device__ __forceinline__ void unpack(uint4 t, uint32_t (&o)[4]) {
-  o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
-}
-__device__ __forceinline__ uint32_t pack(const uint32_t (&o)[1]) { return o[0]; }
-__device__ __forceinline__ uint2 pack(const uint32_t (&o)[2]) { return make_uint2(o[0], o[1]); }
-__device__ __forceinline__ uint4 pack(const uint32_t (&o)[4]) {
-  return make_uint4(o[0], o[1], o[2], o[3]);
-}
-
-/* read-only path (other colour, couplings) */
-template <int VW>
-__device__ __forceinline__ void ld_ro(const uint32_t *p, uint32_t (&o)[VW]) {
-  unpack(__ldg(reinterpret_cast<const typename vt<VW>::T *>(p)), o);
-}
-/* own colour: read then written back by the same thread */
-template <int VW>
-__device__ __forceinline__ void ld_rw(const uint32_t *p, uint32_t (&o)[VW]) {
-  unpack(*reinterpret_cast<const typename vt<VW>::T *>(p), o);
-}
-template <int VW>
-__device__ __forceinline__ void st_rw(uint32_t *p, const uint32_t (&o)[VW]) {
-  *reinterpret_cast<typename vt<VW>::T *>(p) = pack(o);
-}
-/* demon planes: touched once per iteration, streamed (evict-first) */
-template <int VW>
-__device__ __forceinline__ void ld_stream(const uint32_t *p, uint32_t (&o)[VW]) {
-  unpack(__ldcs(reinterpret_cast<const typename vt<VW>::T *>(p)), o);
-}
-template <int VW>
-__device__ __forceinline__ void st_stream(uint32_t *p, const uint32_t (&o)[VW]) {
-  __stcs(reinterpret_cast<typename vt<VW>::T *>(p), pack(o));
-}
-
+/* ------------------------------------------------------- memory access */
 /* L2 residency policies for the sweeps: the spin lattice and the coupling
  * bytes (re-read by every half-sweep) are kept with evict_last; the demon
  * planes (touched once per iteration) are streamed with evict_first. */
@@ -209,15 +169,34 @@ __device__ __forceinline__ uint32_t metropolis_flip(uint32_t j1, uint32_t j2, ui
   return (j1 & j3 & id1) | ((j24 | id2) & (j1 | j3 | id1)) | ((j2 & j4) | (j24 & id2));
 }
 
-/* One thread = one site of colour p and VW replica words of it (group grp of
- * G = W/VW).  Block = (TX sites along x/2) x (TY rows); TX divides L/2, so no
- * thread index needs a division.  grid = (L/2/TX, ytiles*ns*G, L): sample,
- * row tile and word group come from the block index, z from blockIdx.z.
- * In-plane offsets are 32-bit (P*W < 2^32 is checked at creation). */
+/* Inputs of one site for one z step (VW replica words each). */
+template <int VW> struct site_in {
+  uint32_t own[VW], up[VW], vx[VW], vn[VW], vs[VW], a0[VW], a1[VW], a2[VW];
+  uint32_t jbits;
+};
+
+/* Half-sweep of colour p.  One thread owns the column (x/2, y) of one sample
+ * and VW replica words of it (group grp of G = W/VW), and marches over the z
+ * chunk [z0, z0 + zc).  Block = (TX along x/2) x (TY rows); TX divides L/2,
+ * grid = (L/2/TX, ytiles*ns*G, L/zc).
+ *
+ * Along a column the other-colour word at (x/2, y, z) is the x-neighbour of
+ * the site at z and the z-neighbour of the sites at z-1 and z+1: it is loaded
+ * once and kept in registers (vm, v0, up).  The second x-neighbour (x/2 +-1)
+ * and the two y-neighbours are loads that hit L1 (other threads' words).
+ * Loads of step t+1 are issued before the arithmetic of step t.
+ *
+ * Which x-neighbour is +x alternates with z; the update depends only on the
+ * total number of unsatisfied bonds u (the ISI algebra and the Metropolis
+ * rule are both functions of u = (j1+2 j2) + (j3+2 j4), checked over their
+ * whole truth tables in tests/test_host_cpu.py), so the word at x/2 always
+ * enters the second group and the other x-neighbour the first, each with its
+ * own coupling bit.  In-plane offsets are 32-bit (P*W < 2^32 is checked at
+ * creation). */
 template <int VW, bool MICSA>
 __global__ void __launch_bounds__(TPB)
 k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
-        uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
+        const int zc, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
         uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
         const int *__restrict__ walk, const uint32_t *__restrict__ rnd) {
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
@@ -227,86 +206,114 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
   const uint32_t y = tile * blockDim.y + threadIdx.y;
   if (y >= L) return;
   const uint32_t xh = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t z = blockIdx.z;
   const uint32_t plane = L * Lh;
-  const uint32_t i = (z * L + y) * Lh + xh;
-  const uint32_t rowoff = (y + z + p) & 1; /* x = 2*xh + rowoff */
-  /* other-colour neighbours: +x is at x/2 + rowoff, -x at x/2 + rowoff - 1 */
-  const uint32_t iE = rowoff ? (xh + 1 == Lh ? i + 1 - Lh : i + 1) : i;
-  const uint32_t iO = rowoff ? i : (xh == 0 ? i + Lh - 1 : i - 1);
-  const uint32_t iN = (y + 1 == L) ? i - (L - 1) * Lh : i + Lh;
-  const uint32_t iS = (y == 0) ? i + (L - 1) * Lh : i - Lh;
-  const uint32_t iU = (z + 1 == L) ? i - (L - 1) * plane : i + plane;
-  const uint32_t iD = (z == 0) ? i + (L - 1) * plane : i - plane;
+  const uint32_t z0 = blockIdx.z * zc;
+  /* in-plane indices of the column and of its other-colour neighbours */
+  const uint32_t row = y * Lh + xh;
+  const uint32_t rowN = (y + 1 == L) ? xh : row + Lh;
+  const uint32_t rowS = (y == 0) ? row + (L - 1) * Lh : row - Lh;
+  const uint32_t rowXp = (xh + 1 == Lh) ? row + 1 - Lh : row + 1;
+  const uint32_t rowXm = (xh == 0) ? row + Lh - 1 : row - 1;
   const size_t P = (size_t)g.P;
   uint32_t *mine = spin + (size_t)(s * 2 + p) * P * W + grp * VW;
   const uint32_t *oth = spin + (size_t)(s * 2 + (p ^ 1)) * P * W + grp * VW;
+  const uint8_t *jbp = jb + (size_t)(s * 2 + p) * P;
   const uint64_t keep = l2_keep(), strm = l2_stream();
 
-  uint32_t sv[VW], nE[VW], nN[VW], nU[VW], nO[VW], nS[VW], nD[VW];
-  hint<VW>::ld(mine + i * W, sv, keep);
-  hint<VW>::ld_nc(oth + iE * W, nE, keep);
-  hint<VW>::ld_nc(oth + iN * W, nN, keep);
-  hint<VW>::ld_nc(oth + iU * W, nU, keep);
-  hint<VW>::ld_nc(oth + iO * W, nO, keep);
-  hint<VW>::ld_nc(oth + iS * W, nS, keep);
-  hint<VW>::ld_nc(oth + iD * W, nD, keep);
-  const uint32_t jbits = ld_byte_keep(jb + (size_t)(s * 2 + p) * P + i, keep);
-  const uint32_t m0 = jmask(jbits, 0), m1 = jmask(jbits, 1), m2 = jmask(jbits, 2);
-  const uint32_t m3 = jmask(jbits, 3), m4 = jmask(jbits, 4), m5 = jmask(jbits, 5);
-
-  uint32_t a0[VW], a1[VW], a2[VW];
-  uint32_t *q0 = nullptr, *q1 = nullptr;
+  /* demon plane (p, ic): the demon of site x sits at x - sgn*2k*e_axis after
+   * k walks (see micsa_kernels.cuh) */
+  uint32_t *q0b = nullptr, *q1b = nullptr;
+  uint32_t drow = row, zd = z0;
   if (MICSA) {
-    /* demon of this site after k walks: stored 2k sites back along the
-     * plane's axis (see micsa_kernels.cuh) */
-    const int k = walk[s];
+    const int k = __ldg(walk + s);
     const int sh = ((p == 0) == (ic < 3)) ? k : -k; /* in units of 2 sites */
     const int axis = ic < 3 ? ic : ic - 3;
-    uint32_t slot = i;
     if (axis == 0) {
       int xd = (int)xh - sh;
       xd += xd < 0 ? (int)Lh : (xd >= (int)Lh ? -(int)Lh : 0);
-      slot = i - xh + (uint32_t)xd;
+      drow = y * Lh + (uint32_t)xd;
     } else if (axis == 1) {
       int yd = (int)y - 2 * sh;
       yd += yd < 0 ? (int)L : (yd >= (int)L ? -(int)L : 0);
-      slot = i + (uint32_t)((yd - (int)y) * (int)Lh);
+      drow = (uint32_t)yd * Lh + xh;
     } else {
-      int zd = (int)z - 2 * sh;
-      zd += zd < 0 ? (int)L : (zd >= (int)L ? -(int)L : 0);
-      slot = (uint32_t)((int)i + (zd - (int)z) * (int)plane);
+      int t = (int)z0 - 2 * sh;
+      t += t < 0 ? (int)L : (t >= (int)L ? -(int)L : 0);
+      zd = (uint32_t)t;
     }
     const size_t base = ((size_t)(s * 2 + p) * g.nc + ic) * P * W + grp * VW;
-    q0 = d0 + base + (size_t)slot * W;
-    q1 = d1 + base + (size_t)slot * W;
-    hint<VW>::ld_na(q0, a0, strm);
-    hint<VW>::ld_na(q1, a1, strm);
-  } else {
-    const uint32_t *rb = rnd + (size_t)i * W + grp * VW;
-    hint<VW>::ld_na(rb, a0, strm);
-    hint<VW>::ld_na(rb + P * W, a1, strm);
-    hint<VW>::ld_na(rb + 2 * P * W, a2, strm);
+    q0b = d0 + base;
+    q1b = d1 + base;
   }
 
+  /* other colour at (x/2, y) for planes z0-1 and z0 */
+  uint32_t vm[VW], v0[VW];
+  hint<VW>::ld_nc(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, vm, keep);
+  hint<VW>::ld_nc(oth + (z0 * plane + row) * W, v0, keep);
+
+  auto load = [&](uint32_t z, uint32_t zdz, site_in<VW> &in) {
+    const uint32_t zo = z * plane;
+    const uint32_t rowoff = (y + z + p) & 1; /* x = 2*xh + rowoff */
+    hint<VW>::ld(mine + (zo + row) * W, in.own, keep);
+    hint<VW>::ld_nc(oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, in.up, keep);
+    hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, in.vx, keep);
+    hint<VW>::ld_nc(oth + (zo + rowN) * W, in.vn, keep);
+    hint<VW>::ld_nc(oth + (zo + rowS) * W, in.vs, keep);
+    in.jbits = ld_byte_keep(jbp + zo + row, keep);
+    if (MICSA) {
+      const uint32_t slot = (zdz * plane + drow) * W;
+      hint<VW>::ld_na(q0b + slot, in.a0, strm);
+      hint<VW>::ld_na(q1b + slot, in.a1, strm);
+    } else {
+      const uint32_t *rb = rnd + (size_t)(zo + row) * W + grp * VW;
+      hint<VW>::ld_na(rb, in.a0, strm);
+      hint<VW>::ld_na(rb + P * W, in.a1, strm);
+      hint<VW>::ld_na(rb + 2 * P * W, in.a2, strm);
+    }
+  };
+
+  site_in<VW> cur{}, nxt{};
+  uint32_t zdd = zd;
+  load(z0, zdd, cur);
+#pragma unroll 2
+  for (uint32_t t = 0; t < (uint32_t)zc; t++) {
+    const uint32_t z = z0 + t;
+    const uint32_t zn = (zdd + 1 == L) ? 0 : zdd + 1;
+    if (t + 1 < (uint32_t)zc) load(z + 1, zn, nxt);
+    /* couplings: bits E,N,U,O,S,D; the loaded x-neighbour is +x (bit 0)
+     * when rowoff = 1 and -x (bit 3) otherwise; the word at x/2 is the other */
+    const uint32_t rowoff = (y + z + p) & 1;
+    const uint32_t jb6 = cur.jbits;
+    const uint32_t mX = jmask(jb6, rowoff ? 0 : 3), mV = jmask(jb6, rowoff ? 3 : 0);
+    const uint32_t mN = jmask(jb6, 1), mU = jmask(jb6, 2), mS = jmask(jb6, 4), mD = jmask(jb6, 5);
 #pragma unroll
-  for (int w = 0; w < VW; w++) {
-    const uint32_t sw = sv[w];
-    const uint32_t f0 = sw ^ nE[w] ^ m0, f1 = sw ^ nN[w] ^ m1, f2 = sw ^ nU[w] ^ m2;
-    const uint32_t f3 = sw ^ nO[w] ^ m3, f4 = sw ^ nS[w] ^ m4, f5 = sw ^ nD[w] ^ m5;
-    const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
-    const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
-    uint32_t flip;
-    if (MICSA)
-      flip = isi_update(j1, j2, j3, j4, a0[w], a1[w]);
-    else
-      flip = metropolis_flip(j1, j2, j3, j4, a0[w], a1[w], a2[w]);
-    sv[w] = sw ^ flip;
-  }
-  hint<VW>::st(mine + i * W, sv, keep);
-  if (MICSA) {
-    hint<VW>::st(q0, a0, strm);
-    hint<VW>::st(q1, a1, strm);
+    for (int w = 0; w < VW; w++) {
+      const uint32_t sw = cur.own[w];
+      const uint32_t f0 = sw ^ cur.vx[w] ^ mX, f1 = sw ^ cur.vn[w] ^ mN, f2 = sw ^ cur.up[w] ^ mU;
+      const uint32_t f3 = sw ^ v0[w] ^ mV, f4 = sw ^ cur.vs[w] ^ mS, f5 = sw ^ vm[w] ^ mD;
+      const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
+      const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+      uint32_t flip;
+      if (MICSA)
+        flip = isi_update(j1, j2, j3, j4, cur.a0[w], cur.a1[w]);
+      else
+        flip = metropolis_flip(j1, j2, j3, j4, cur.a0[w], cur.a1[w], cur.a2[w]);
+      cur.own[w] = sw ^ flip;
+    }
+    const uint32_t zo = z * plane;
+    hint<VW>::st(mine + (zo + row) * W, cur.own, keep);
+    if (MICSA) {
+      const uint32_t slot = (zdd * plane + drow) * W;
+      hint<VW>::st(q0b + slot, cur.a0, strm);
+      hint<VW>::st(q1b + slot, cur.a1, strm);
+    }
+#pragma unroll
+    for (int w = 0; w < VW; w++) {
+      vm[w] = v0[w];
+      v0[w] = cur.up[w];
+    }
+    cur = nxt;
+    zdd = zn;
   }
 }
 
@@ -581,12 +588,14 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
   while (g.Lh % tx) tx >>= 1;
   const int ty = TPB / tx;
   const int ytiles = (g.L + ty - 1) / ty;
+  /* z chunk per thread: long columns at large L, more threads at small L */
+  const int zc = g.zc > 0 ? g.zc : ((g.L >= 128 && g.L % 16 == 0) ? 16 : (g.L >= 48 ? 8 : 2));
   dim3 block(tx, ty);
-  dim3 grid(g.Lh / tx, ytiles * g.ns * G, g.L);
+  dim3 grid(g.Lh / tx, ytiles * g.ns * G, g.L / zc);
   if (micsa)
-    k_sweep<VW, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, spin, d0, d1, jb, walk, rnd);
+    k_sweep<VW, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, spin, d0, d1, jb, walk, rnd);
   else
-    k_sweep<VW, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, spin, d0, d1, jb, walk, rnd);
+    k_sweep<VW, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, spin, d0, d1, jb, walk, rnd);
   return cudaGetLastError();
 }
 
@@ -662,4 +671,11 @@ cudaError_t micsa_launch_overlap(const micsa_geo &g, const uint32_t *spin, unsig
   dim3 grid(measure_blocks(2 * g.P, (int64_t)3 * nd * g.W * g.ns), 3 * nd, g.ns * g.W);
   k_overlap<<<grid, TPB, 0, st>>>(g, spin, qd, c4d);
   return cudaGetLastError();
+}
+
+int micsa_sweep_zc_candidates(int L, int *out, int max) {
+  int n = 0;
+  for (int zc = 1; zc <= 64 && zc <= L && n < max; zc <<= 1)
+    if (L % zc == 0) out[n++] = zc;
+  return n;
 }

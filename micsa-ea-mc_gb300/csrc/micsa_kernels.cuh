@@ -26,7 +26,11 @@ struct micsa_geo {
   int L, Lh, W, nc, ns, nr;
   int64_t P;  /* sites per colour */
   int64_t H;  /* reference words per colour, (L/4)^3/2 */
+  int zc;     /* z planes per thread in the sweeps (divides L; 0 = default) */
 };
+
+/* slab depths the sweep can use for this L (divisors of L, ascending) */
+int micsa_sweep_zc_candidates(int L, int *out, int max);
 
 /* flag = 1 half-sweep of colour p on demon plane ic, all samples */
 cudaError_t micsa_launch_sweep_micsa(const micsa_geo &g, int p, int ic,

@@ -21,8 +21,8 @@ ABI_SYMBOLS = [
     "micsa_create", "micsa_destroy", "micsa_last_error", "micsa_footprint_bytes",
     "micsa_set_lut", "micsa_upload_couplings", "micsa_upload_spins", "micsa_upload_demons",
     "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
-    "micsa_download_demons", "micsa_profile", "micsa_synchronize", "micsa_kernel_launches",
-    "micsa_stream",
+    "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_synchronize",
+    "micsa_kernel_launches", "micsa_stream",
 ]
 
 _lib = None
@@ -84,6 +84,7 @@ def lib():
         "micsa_download_demons": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
         "micsa_profile": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double),
                                     C.POINTER(C.c_double)]),
+        "micsa_tuning_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
         "micsa_synchronize": (C.c_int, [C.c_void_p]),
         "micsa_kernel_launches": (C.c_int64, [C.c_void_p]),
         "micsa_stream": (C.c_void_p, [C.c_void_p]),
@@ -218,6 +219,12 @@ class Context:
         a, b = C.c_double(), C.c_double()
         check(self.h, lib().micsa_profile(self.h, n, C.byref(a), C.byref(b)), "profile")
         return a.value, b.value
+
+    def tuning(self):
+        """The autotuner's choice and timings, as a text line."""
+        buf = C.create_string_buffer(512)
+        check(self.h, lib().micsa_tuning_report(self.h, buf, 512), "tuning_report")
+        return buf.value.decode()
 
     def kernel_launches(self):
         return lib().micsa_kernel_launches(self.h)

@@ -74,6 +74,24 @@ def test_isi_algebra_is_the_integer_demon_rule():
         assert ((n0 >> i) & 1) + 2 * ((n1 >> i) & 1) == nd
 
 
+def test_metropolis_rule_depends_only_on_total_unsatisfied():
+    """The Metropolis acceptance expression of the reference (main.cu:950-957)
+    is a function of u = (j1 + 2 j2) + (j3 + 2 j4) and the random bits only;
+    with the ISI check above this is why the GPU sweep may put either
+    x-neighbour into either bond group."""
+    seen = {}
+    for a in range(4):
+        for b in range(4):
+            for r in range(8):
+                j1, j2, j3, j4 = a & 1, a >> 1, b & 1, b >> 1
+                b0, b1, b2 = r & 1, (r >> 1) & 1, (r >> 2) & 1
+                b1 &= b0
+                b2 &= b1
+                id2, id1, j24 = b1, (b0 ^ b1) | b2, j2 | j4
+                f = (j1 & j3 & id1) | ((j24 | id2) & (j1 | j3 | id1)) | ((j2 & j4) | (j24 & id2))
+                assert seen.setdefault((a + b, r), f) == f
+
+
 @pytest.mark.parametrize("L", [8, 16, 24, 40])
 def test_pack_unpack_roundtrip(L):
     """check_packing (ini.c:397-423)."""
