@@ -17,6 +17,8 @@
 #include "micsa.h"
 #include "micsa_kernels.cuh"
 
+#define MICSA_TUNE_MAX 24
+
 struct micsa_ctx {
   micsa_config cfg;
   micsa_geo g;
@@ -33,9 +35,9 @@ struct micsa_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int64_t launches = 0;
-  int ntune = 0;           /* slab-depth candidates timed at creation */
-  int tune_zc[8] = {0};
-  double tune_ms[8] = {0};
+  int ntune = 0;           /* launch shapes timed at creation */
+  int tune_zc[MICSA_TUNE_MAX] = {0}, tune_pd[MICSA_TUNE_MAX] = {0};
+  double tune_ms[MICSA_TUNE_MAX] = {0};
   char err[512] = {0};
 };
 
@@ -144,35 +146,46 @@ int ready_for_sweeps(micsa_ctx *ctx, int need_demons) {
  * way); only the speed does. */
 int autotune(micsa_ctx *ctx) {
   micsa_geo &g = ctx->g;
-  int cand[8];
-  const int n = micsa_sweep_zc_candidates(g.L, cand, 8);
+  int zcs[8];
+  const int nz = micsa_sweep_zc_candidates(g.L, zcs, 8);
+  const int pds[3] = {0, 2, 4};
   cudaEvent_t e0, e1;
   MICSA_CK(cudaEventCreate(&e0));
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
-  int best_zc = cand[n - 1];
+  int best_zc = zcs[nz - 1], best_pd = 0, n = 0;
   const int reps = 4;
-  for (int c = 0; c < n; c++) {
-    g.zc = cand[c];
-    for (int rep = -1; rep < reps; rep++) { /* rep -1: warm-up */
-      if (rep == 0) MICSA_CK(cudaEventRecord(e0, ctx->stream));
-      for (int p = 0; p < 2; p++)
-        MICSA_CK(micsa_launch_sweep_micsa(g, p, 0, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
-                                          ctx->walk, ctx->stream));
+  for (int c = 0; c < nz; c++)
+    for (int d = 0; d < 3; d++) {
+      if (pds[d] && pds[d] >= zcs[c]) continue; /* prefetch only within a slab */
+      g.zc = zcs[c];
+      g.pd = pds[d];
+      for (int rep = -1; rep < reps; rep++) { /* rep -1: warm-up */
+        if (rep == 0) MICSA_CK(cudaEventRecord(e0, ctx->stream));
+        for (int p = 0; p < 2; p++)
+          MICSA_CK(micsa_launch_sweep_micsa(g, p, 0, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
+                                            ctx->walk, ctx->stream));
+      }
+      MICSA_CK(cudaEventRecord(e1, ctx->stream));
+      MICSA_CK(cudaEventSynchronize(e1));
+      float ms = 0;
+      MICSA_CK(cudaEventElapsedTime(&ms, e0, e1));
+      const double per = ms / (2.0 * reps);
+      if (n < MICSA_TUNE_MAX) {
+        ctx->tune_zc[n] = g.zc;
+        ctx->tune_pd[n] = g.pd;
+        ctx->tune_ms[n] = per;
+        n++;
+      }
+      if (per < best) {
+        best = per;
+        best_zc = g.zc;
+        best_pd = g.pd;
+      }
     }
-    MICSA_CK(cudaEventRecord(e1, ctx->stream));
-    MICSA_CK(cudaEventSynchronize(e1));
-    float ms = 0;
-    MICSA_CK(cudaEventElapsedTime(&ms, e0, e1));
-    ctx->tune_zc[c] = cand[c];
-    ctx->tune_ms[c] = ms / (2.0 * reps);
-    if (ctx->tune_ms[c] < best) {
-      best = ctx->tune_ms[c];
-      best_zc = cand[c];
-    }
-  }
   ctx->ntune = n;
   g.zc = best_zc;
+  g.pd = best_pd;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return MICSA_OK;
@@ -222,6 +235,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.nr = cfg->nr;
   g.P = s.P;
   g.zc = 0;
+  g.pd = 0;
   g.H = s.H;
   ctx->stage_words = (size_t)s.stage_w;
   ctx->acc_words = (size_t)s.acc_w;
@@ -272,9 +286,10 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d", ctx->g.zc);
+  int k = snprintf(buf, n, "zc=%d pd=%d |", ctx->g.zc, ctx->g.pd);
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
-    k += snprintf(buf + k, n - (size_t)k, " %d:%.5fms", ctx->tune_zc[c], ctx->tune_ms[c]);
+    k += snprintf(buf + k, n - (size_t)k, " %d/%d:%.5fms", ctx->tune_zc[c], ctx->tune_pd[c],
+                  ctx->tune_ms[c]);
   return MICSA_OK;
 }
 

@@ -84,6 +84,9 @@ template <> struct hint<4> {
                  :: "l"(a), "r"(o[0]), "r"(o[1]), "r"(o[2]), "r"(o[3]), "l"(pol) : "memory");
   }
 };
+__device__ __forceinline__ void prefetch_l2(const uint32_t *a) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+}
 __device__ __forceinline__ uint32_t ld_byte_keep(const uint8_t *a, uint64_t pol) {
   uint32_t v;
   asm("ld.global.nc.L2::cache_hint.u8 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
@@ -196,7 +199,7 @@ template <int VW> struct site_in {
 template <int VW, bool MICSA>
 __global__ void __launch_bounds__(TPB)
 k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
-        const int zc, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
+        const int zc, const int pd, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
         uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
         const int *__restrict__ walk, const uint32_t *__restrict__ rnd) {
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
@@ -279,6 +282,22 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
   for (uint32_t t = 0; t < (uint32_t)zc; t++) {
     const uint32_t z = z0 + t;
     const uint32_t zn = (zdd + 1 == L) ? 0 : zdd + 1;
+    /* the demon (or random) words are the only DRAM stream: ask L2 for the
+     * ones pd steps ahead so that the loads below find them there */
+    if (pd > 0 && t + (uint32_t)pd < (uint32_t)zc) {
+      uint32_t zf = zdd + (uint32_t)pd;
+      if (zf >= L) zf -= L;
+      if (MICSA) {
+        const uint32_t slot = (zf * plane + drow) * W;
+        prefetch_l2(q0b + slot);
+        prefetch_l2(q1b + slot);
+      } else {
+        const uint32_t *rb = rnd + (size_t)((z + pd) * plane + row) * W + grp * VW;
+        prefetch_l2(rb);
+        prefetch_l2(rb + P * W);
+        prefetch_l2(rb + 2 * P * W);
+      }
+    }
     if (t + 1 < (uint32_t)zc) load(z + 1, zn, nxt);
     /* couplings: bits E,N,U,O,S,D; the loaded x-neighbour is +x (bit 0)
      * when rowoff = 1 and -x (bit 3) otherwise; the word at x/2 is the other */
@@ -593,9 +612,9 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
   dim3 block(tx, ty);
   dim3 grid(g.Lh / tx, ytiles * g.ns * G, g.L / zc);
   if (micsa)
-    k_sweep<VW, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, spin, d0, d1, jb, walk, rnd);
+    k_sweep<VW, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
   else
-    k_sweep<VW, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, spin, d0, d1, jb, walk, rnd);
+    k_sweep<VW, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
   return cudaGetLastError();
 }
 

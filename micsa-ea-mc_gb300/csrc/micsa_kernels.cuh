@@ -27,6 +27,7 @@ struct micsa_geo {
   int64_t P;  /* sites per colour */
   int64_t H;  /* reference words per colour, (L/4)^3/2 */
   int zc;     /* z planes per thread in the sweeps (divides L; 0 = default) */
+  int pd;     /* L2 prefetch distance of the demon stream, in z steps (0 = off) */
 };
 
 /* slab depths the sweep can use for this L (divisors of L, ascending) */
