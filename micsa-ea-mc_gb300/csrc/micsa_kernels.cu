@@ -172,51 +172,79 @@ __device__ __forceinline__ uint32_t metropolis_flip(uint32_t j1, uint32_t j2, ui
   return (j1 & j3 & id1) | ((j24 | id2) & (j1 | j3 | id1)) | ((j2 & j4) | (j24 & id2));
 }
 
-/* Inputs of one site for one z step (VW replica words each). */
-template <int VW> struct site_in {
-  uint32_t own[VW], up[VW], vx[VW], vn[VW], vs[VW], a0[VW], a1[VW], a2[VW];
-  uint32_t jbits;
+/* Loads of 2*VW consecutive words (the same VW words of two adjacent sites). */
+template <int VW> struct pair_io;
+template <> struct pair_io<1> {
+  static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[2], uint64_t p) { hint<2>::ld_nc(a, o, p); }
+  static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[2], uint64_t p) { hint<2>::ld(a, o, p); }
+  static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t (&o)[2], uint64_t p) { hint<2>::ld_na(a, o, p); }
+  static __device__ __forceinline__ void st(uint32_t *a, const uint32_t (&o)[2], uint64_t p) { hint<2>::st(a, o, p); }
 };
+template <> struct pair_io<2> {
+  static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[4], uint64_t p) { hint<4>::ld_nc(a, o, p); }
+  static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[4], uint64_t p) { hint<4>::ld(a, o, p); }
+  static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t (&o)[4], uint64_t p) { hint<4>::ld_na(a, o, p); }
+  static __device__ __forceinline__ void st(uint32_t *a, const uint32_t (&o)[4], uint64_t p) { hint<4>::st(a, o, p); }
+};
+template <> struct pair_io<4> {
+  static __device__ __forceinline__ void split(const uint32_t (&o)[8], uint32_t (&a)[4], uint32_t (&b)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) { a[k] = o[k]; b[k] = o[4 + k]; }
+  }
+  static __device__ __forceinline__ void join(uint32_t (&o)[8], const uint32_t (&a)[4], const uint32_t (&b)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) { o[k] = a[k]; o[4 + k] = b[k]; }
+  }
+  static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[8], uint64_t p) {
+    uint32_t x[4], y[4]; hint<4>::ld_nc(a, x, p); hint<4>::ld_nc(a + 4, y, p); join(o, x, y);
+  }
+  static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[8], uint64_t p) {
+    uint32_t x[4], y[4]; hint<4>::ld(a, x, p); hint<4>::ld(a + 4, y, p); join(o, x, y);
+  }
+  static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t (&o)[8], uint64_t p) {
+    uint32_t x[4], y[4]; hint<4>::ld_na(a, x, p); hint<4>::ld_na(a + 4, y, p); join(o, x, y);
+  }
+  static __device__ __forceinline__ void st(uint32_t *a, const uint32_t (&o)[8], uint64_t p) {
+    uint32_t x[4], y[4]; split(o, x, y); hint<4>::st(a, x, p); hint<4>::st(a + 4, y, p);
+  }
+};
+__device__ __forceinline__ uint32_t ld_u16_keep(const uint8_t *a, uint64_t pol) {
+  uint32_t v;
+  asm("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
 
-/* Half-sweep of colour p.  One thread owns the column (x/2, y) of one sample
- * and VW replica words of it (group grp of G = W/VW), and marches over the z
- * chunk [z0, z0 + zc).  Block = (TX along x/2) x (TY rows); TX divides L/2,
- * grid = (L/2/TX, ytiles*ns*G, L/zc).
- *
- * Along a column the other-colour word at (x/2, y, z) is the x-neighbour of
- * the site at z and the z-neighbour of the sites at z-1 and z+1: it is loaded
- * once and kept in registers (vm, v0, up).  The second x-neighbour (x/2 +-1)
- * and the two y-neighbours are loads that hit L1 (other threads' words).
- * Loads of step t+1 are issued before the arithmetic of step t.
- *
- * Which x-neighbour is +x alternates with z; the update depends only on the
- * total number of unsatisfied bonds u (the ISI algebra and the Metropolis
- * rule are both functions of u = (j1+2 j2) + (j3+2 j4), checked over their
- * whole truth tables in tests/test_host_cpu.py), so the word at x/2 always
- * enters the second group and the other x-neighbour the first, each with its
- * own coupling bit.  In-plane offsets are 32-bit (P*W < 2^32 is checked at
- * creation). */
+/* Half-sweep of colour p.  One thread owns two adjacent columns (x/2 = 2j,
+ * 2j+1; y) of one sample, VW replica words each (group grp of G = W/VW), and
+ * marches over the z chunk [z0, z0 + zc).  The two sites share their row
+ * offset, so each load brings the pair: own spins, the other-colour words at
+ * (2j, 2j+1) of planes z-1, z, z+1 (z-neighbours of the pair and two of its
+ * four x-neighbours; kept in registers along z), the pairs at y+-1, one
+ * extra other-colour word for the remaining x-neighbour, the two coupling
+ * bytes and the two demon words per plane.  Block = (TX pairs along x/2) x
+ * (TY rows); TX divides L/4; grid = (L/4/TX, ytiles*ns*G, L/zc).
+ * In-plane offsets are 32-bit (P*W < 2^32 is checked at creation). */
 template <int VW, bool MICSA>
 __global__ void __launch_bounds__(TPB)
 k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
         const int zc, const int pd, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
         uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
         const int *__restrict__ walk, const uint32_t *__restrict__ rnd) {
+  constexpr int N = 2 * VW; /* words per pair */
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
   const uint32_t by = blockIdx.y;
   const uint32_t tile = by % ytiles, sg = by / ytiles; /* block-uniform */
   const uint32_t s = sg / G, grp = sg % G;
   const uint32_t y = tile * blockDim.y + threadIdx.y;
   if (y >= L) return;
-  const uint32_t xh = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t xa = 2 * (blockIdx.x * blockDim.x + threadIdx.x); /* x/2 of site A */
   const uint32_t plane = L * Lh;
   const uint32_t z0 = blockIdx.z * zc;
-  /* in-plane indices of the column and of its other-colour neighbours */
-  const uint32_t row = y * Lh + xh;
-  const uint32_t rowN = (y + 1 == L) ? xh : row + Lh;
+  const uint32_t row = y * Lh + xa;
+  const uint32_t rowN = (y + 1 == L) ? xa : row + Lh;
   const uint32_t rowS = (y == 0) ? row + (L - 1) * Lh : row - Lh;
-  const uint32_t rowXp = (xh + 1 == Lh) ? row + 1 - Lh : row + 1;
-  const uint32_t rowXm = (xh == 0) ? row + Lh - 1 : row - 1;
+  const uint32_t rowXp = (xa + 2 == Lh) ? row + 2 - Lh : row + 2; /* x/2 = 2j+2 */
+  const uint32_t rowXm = (xa == 0) ? row + Lh - 1 : row - 1;      /* x/2 = 2j-1 */
   const size_t P = (size_t)g.P;
   uint32_t *mine = spin + (size_t)(s * 2 + p) * P * W + grp * VW;
   const uint32_t *oth = spin + (size_t)(s * 2 + (p ^ 1)) * P * W + grp * VW;
@@ -224,21 +252,27 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
   const uint64_t keep = l2_keep(), strm = l2_stream();
 
   /* demon plane (p, ic): the demon of site x sits at x - sgn*2k*e_axis after
-   * k walks (see micsa_kernels.cuh) */
+   * k walks (see micsa_kernels.cuh).  An x shift by an odd number of x/2
+   * steps separates the pair's two demon words (and may wrap between them). */
   uint32_t *q0b = nullptr, *q1b = nullptr;
-  uint32_t drow = row, zd = z0;
+  uint32_t drowA = row, drowB = row + 1, zd = z0;
+  bool dpair = true;
   if (MICSA) {
     const int k = __ldg(walk + s);
     const int sh = ((p == 0) == (ic < 3)) ? k : -k; /* in units of 2 sites */
     const int axis = ic < 3 ? ic : ic - 3;
     if (axis == 0) {
-      int xd = (int)xh - sh;
+      int xd = (int)xa - sh;
       xd += xd < 0 ? (int)Lh : (xd >= (int)Lh ? -(int)Lh : 0);
-      drow = y * Lh + (uint32_t)xd;
+      const int xe = (xd + 1 == (int)Lh) ? 0 : xd + 1;
+      drowA = y * Lh + (uint32_t)xd;
+      drowB = y * Lh + (uint32_t)xe;
+      dpair = !(sh & 1);
     } else if (axis == 1) {
       int yd = (int)y - 2 * sh;
       yd += yd < 0 ? (int)L : (yd >= (int)L ? -(int)L : 0);
-      drow = (uint32_t)yd * Lh + xh;
+      drowA = (uint32_t)yd * Lh + xa;
+      drowB = drowA + 1;
     } else {
       int t = (int)z0 - 2 * sh;
       t += t < 0 ? (int)L : (t >= (int)L ? -(int)L : 0);
@@ -249,90 +283,108 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
     q1b = d1 + base;
   }
 
-  /* other colour at (x/2, y) for planes z0-1 and z0 */
-  uint32_t vm[VW], v0[VW];
-  hint<VW>::ld_nc(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, vm, keep);
-  hint<VW>::ld_nc(oth + (z0 * plane + row) * W, v0, keep);
+  /* other colour at (2j, 2j+1; y) for planes z0-1 and z0 */
+  uint32_t vm[N], v0[N];
+  pair_io<VW>::ld_nc(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, vm, keep);
+  pair_io<VW>::ld_nc(oth + (z0 * plane + row) * W, v0, keep);
 
-  auto load = [&](uint32_t z, uint32_t zdz, site_in<VW> &in) {
-    const uint32_t zo = z * plane;
-    const uint32_t rowoff = (y + z + p) & 1; /* x = 2*xh + rowoff */
-    hint<VW>::ld(mine + (zo + row) * W, in.own, keep);
-    hint<VW>::ld_nc(oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, in.up, keep);
-    hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, in.vx, keep);
-    hint<VW>::ld_nc(oth + (zo + rowN) * W, in.vn, keep);
-    hint<VW>::ld_nc(oth + (zo + rowS) * W, in.vs, keep);
-    in.jbits = ld_byte_keep(jbp + zo + row, keep);
-    if (MICSA) {
-      const uint32_t slot = (zdz * plane + drow) * W;
-      hint<VW>::ld_na(q0b + slot, in.a0, strm);
-      hint<VW>::ld_na(q1b + slot, in.a1, strm);
-    } else {
-      const uint32_t *rb = rnd + (size_t)(zo + row) * W + grp * VW;
-      hint<VW>::ld_na(rb, in.a0, strm);
-      hint<VW>::ld_na(rb + P * W, in.a1, strm);
-      hint<VW>::ld_na(rb + 2 * P * W, in.a2, strm);
-    }
-  };
-
-  site_in<VW> cur{}, nxt{};
   uint32_t zdd = zd;
-  load(z0, zdd, cur);
 #pragma unroll 2
   for (uint32_t t = 0; t < (uint32_t)zc; t++) {
     const uint32_t z = z0 + t;
-    const uint32_t zn = (zdd + 1 == L) ? 0 : zdd + 1;
-    /* the demon (or random) words are the only DRAM stream: ask L2 for the
-     * ones pd steps ahead so that the loads below find them there */
-    if (pd > 0 && t + (uint32_t)pd < (uint32_t)zc) {
-      uint32_t zf = zdd + (uint32_t)pd;
-      if (zf >= L) zf -= L;
-      if (MICSA) {
-        const uint32_t slot = (zf * plane + drow) * W;
-        prefetch_l2(q0b + slot);
-        prefetch_l2(q1b + slot);
+    const uint32_t zo = z * plane;
+    const uint32_t rowoff = (y + z + p) & 1; /* x = 2*(x/2) + rowoff for both */
+    uint32_t own[N], up[N], vn[N], vs[N], ext[VW], a0[N], a1[N], a2[N];
+    pair_io<VW>::ld(mine + (zo + row) * W, own, keep);
+    pair_io<VW>::ld_nc(oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, up, keep);
+    pair_io<VW>::ld_nc(oth + (zo + rowN) * W, vn, keep);
+    pair_io<VW>::ld_nc(oth + (zo + rowS) * W, vs, keep);
+    hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
+    const uint32_t jb2 = ld_u16_keep(jbp + zo + row, keep);
+    if (MICSA) {
+      const uint32_t sa = (zdd * plane + drowA) * W;
+      if (dpair) {
+        pair_io<VW>::ld_na(q0b + sa, a0, strm);
+        pair_io<VW>::ld_na(q1b + sa, a1, strm);
       } else {
-        const uint32_t *rb = rnd + (size_t)((z + pd) * plane + row) * W + grp * VW;
-        prefetch_l2(rb);
-        prefetch_l2(rb + P * W);
-        prefetch_l2(rb + 2 * P * W);
+        const uint32_t sb = (zdd * plane + drowB) * W;
+        uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
+        hint<VW>::ld_na(q0b + sa, x0, strm);
+        hint<VW>::ld_na(q0b + sb, x1, strm);
+        hint<VW>::ld_na(q1b + sa, y0, strm);
+        hint<VW>::ld_na(q1b + sb, y1, strm);
+#pragma unroll
+        for (int w = 0; w < VW; w++) {
+          a0[w] = x0[w]; a0[VW + w] = x1[w];
+          a1[w] = y0[w]; a1[VW + w] = y1[w];
+        }
+      }
+      if (pd > 0 && t + (uint32_t)pd < (uint32_t)zc) {
+        uint32_t zf = zdd + (uint32_t)pd;
+        if (zf >= L) zf -= L;
+        prefetch_l2(q0b + (zf * plane + drowA) * W);
+        prefetch_l2(q1b + (zf * plane + drowA) * W);
+      }
+    } else {
+      const uint32_t *rb = rnd + (size_t)(zo + row) * W + grp * VW;
+      pair_io<VW>::ld_na(rb, a0, strm);
+      pair_io<VW>::ld_na(rb + P * W, a1, strm);
+      pair_io<VW>::ld_na(rb + 2 * P * W, a2, strm);
+    }
+    /* x-neighbours: site A (x/2 = 2j) and B (2j+1) of colour p see, in the
+     * other colour, +x at x/2 + rowoff and -x at x/2 + rowoff - 1 */
+#pragma unroll
+    for (int site = 0; site < 2; site++) {
+      const uint32_t jb6 = (jb2 >> (8 * site)) & 0xffu;
+      const uint32_t mE = jmask(jb6, 0), mN = jmask(jb6, 1), mU = jmask(jb6, 2);
+      const uint32_t mO = jmask(jb6, 3), mS = jmask(jb6, 4), mD = jmask(jb6, 5);
+#pragma unroll
+      for (int w = 0; w < VW; w++) {
+        const int o = site * VW + w;
+        /* A: +x = rowoff ? v0[B] : v0[A], -x = rowoff ? v0[A] : ext
+         * B: +x = rowoff ? ext : v0[B],   -x = rowoff ? v0[B] : v0[A] */
+        const uint32_t cA = v0[w], cB = v0[VW + w], ex = ext[w];
+        const uint32_t nE = site == 0 ? (rowoff ? cB : cA) : (rowoff ? ex : cB);
+        const uint32_t nO = site == 0 ? (rowoff ? cA : ex) : (rowoff ? cB : cA);
+        const uint32_t sw = own[o];
+        const uint32_t f0 = sw ^ nE ^ mE, f1 = sw ^ vn[o] ^ mN, f2 = sw ^ up[o] ^ mU;
+        const uint32_t f3 = sw ^ nO ^ mO, f4 = sw ^ vs[o] ^ mS, f5 = sw ^ vm[o] ^ mD;
+        const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
+        const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+        uint32_t flip;
+        if (MICSA)
+          flip = isi_update(j1, j2, j3, j4, a0[o], a1[o]);
+        else
+          flip = metropolis_flip(j1, j2, j3, j4, a0[o], a1[o], a2[o]);
+        own[o] = sw ^ flip;
       }
     }
-    if (t + 1 < (uint32_t)zc) load(z + 1, zn, nxt);
-    /* couplings: bits E,N,U,O,S,D; the loaded x-neighbour is +x (bit 0)
-     * when rowoff = 1 and -x (bit 3) otherwise; the word at x/2 is the other */
-    const uint32_t rowoff = (y + z + p) & 1;
-    const uint32_t jb6 = cur.jbits;
-    const uint32_t mX = jmask(jb6, rowoff ? 0 : 3), mV = jmask(jb6, rowoff ? 3 : 0);
-    const uint32_t mN = jmask(jb6, 1), mU = jmask(jb6, 2), mS = jmask(jb6, 4), mD = jmask(jb6, 5);
-#pragma unroll
-    for (int w = 0; w < VW; w++) {
-      const uint32_t sw = cur.own[w];
-      const uint32_t f0 = sw ^ cur.vx[w] ^ mX, f1 = sw ^ cur.vn[w] ^ mN, f2 = sw ^ cur.up[w] ^ mU;
-      const uint32_t f3 = sw ^ v0[w] ^ mV, f4 = sw ^ cur.vs[w] ^ mS, f5 = sw ^ vm[w] ^ mD;
-      const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
-      const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
-      uint32_t flip;
-      if (MICSA)
-        flip = isi_update(j1, j2, j3, j4, cur.a0[w], cur.a1[w]);
-      else
-        flip = metropolis_flip(j1, j2, j3, j4, cur.a0[w], cur.a1[w], cur.a2[w]);
-      cur.own[w] = sw ^ flip;
-    }
-    const uint32_t zo = z * plane;
-    hint<VW>::st(mine + (zo + row) * W, cur.own, keep);
+    pair_io<VW>::st(mine + (zo + row) * W, own, keep);
     if (MICSA) {
-      const uint32_t slot = (zdd * plane + drow) * W;
-      hint<VW>::st(q0b + slot, cur.a0, strm);
-      hint<VW>::st(q1b + slot, cur.a1, strm);
+      const uint32_t sa = (zdd * plane + drowA) * W;
+      if (dpair) {
+        pair_io<VW>::st(q0b + sa, a0, strm);
+        pair_io<VW>::st(q1b + sa, a1, strm);
+      } else {
+        const uint32_t sb = (zdd * plane + drowB) * W;
+        uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
+#pragma unroll
+        for (int w = 0; w < VW; w++) {
+          x0[w] = a0[w]; x1[w] = a0[VW + w];
+          y0[w] = a1[w]; y1[w] = a1[VW + w];
+        }
+        hint<VW>::st(q0b + sa, x0, strm);
+        hint<VW>::st(q0b + sb, x1, strm);
+        hint<VW>::st(q1b + sa, y0, strm);
+        hint<VW>::st(q1b + sb, y1, strm);
+      }
     }
 #pragma unroll
-    for (int w = 0; w < VW; w++) {
+    for (int w = 0; w < N; w++) {
       vm[w] = v0[w];
-      v0[w] = cur.up[w];
+      v0[w] = up[w];
     }
-    cur = nxt;
-    zdd = zn;
+    zdd = (zdd + 1 == L) ? 0 : zdd + 1;
   }
 }
 
@@ -601,16 +653,16 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
                             uint32_t *d0, uint32_t *d1, const uint8_t *jb, const int *walk,
                             const uint32_t *rnd, cudaStream_t st) {
   const int G = g.W / VW;
-  /* TX sites along x/2 per block row: the largest power of two <= 32 that
-   * divides L/2 (L/2 is a multiple of 4) */
+  /* TX site pairs along x/2 per block row: the largest power of two <= 32
+   * that divides L/4 (L/4 is even) */
   int tx = 32;
-  while (g.Lh % tx) tx >>= 1;
+  while ((g.Lh / 2) % tx) tx >>= 1;
   const int ty = TPB / tx;
   const int ytiles = (g.L + ty - 1) / ty;
   /* z chunk per thread: long columns at large L, more threads at small L */
   const int zc = g.zc > 0 ? g.zc : ((g.L >= 128 && g.L % 16 == 0) ? 16 : (g.L >= 48 ? 8 : 2));
   dim3 block(tx, ty);
-  dim3 grid(g.Lh / tx, ytiles * g.ns * G, g.L / zc);
+  dim3 grid(g.Lh / 2 / tx, ytiles * g.ns * G, g.L / zc);
   if (micsa)
     k_sweep<VW, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
   else
