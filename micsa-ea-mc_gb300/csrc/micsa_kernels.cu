@@ -214,6 +214,43 @@ __device__ __forceinline__ uint32_t ld_u16_keep(const uint8_t *a, uint64_t pol) 
   return v;
 }
 
+/* The two sites of a pair: with one word group per site (WIDE, G = 1) their
+ * words are adjacent and move as one vector; otherwise they are W words
+ * apart and move as two vectors. */
+template <int VW, bool WIDE> struct pairs {
+  static constexpr int N = 2 * VW;
+  static __device__ __forceinline__ void cat(uint32_t (&o)[N], const uint32_t (&a)[VW],
+                                             const uint32_t (&b)[VW]) {
+#pragma unroll
+    for (int k = 0; k < VW; k++) { o[k] = a[k]; o[VW + k] = b[k]; }
+  }
+  static __device__ __forceinline__ void cut(const uint32_t (&o)[N], uint32_t (&a)[VW],
+                                             uint32_t (&b)[VW]) {
+#pragma unroll
+    for (int k = 0; k < VW; k++) { a[k] = o[k]; b[k] = o[VW + k]; }
+  }
+  static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t W, uint32_t (&o)[N], uint64_t p) {
+    if (WIDE) { pair_io<VW>::ld_nc(a, o, p); return; }
+    uint32_t x[VW], y[VW];
+    hint<VW>::ld_nc(a, x, p); hint<VW>::ld_nc(a + W, y, p); cat(o, x, y);
+  }
+  static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t W, uint32_t (&o)[N], uint64_t p) {
+    if (WIDE) { pair_io<VW>::ld(a, o, p); return; }
+    uint32_t x[VW], y[VW];
+    hint<VW>::ld(a, x, p); hint<VW>::ld(a + W, y, p); cat(o, x, y);
+  }
+  static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t W, uint32_t (&o)[N], uint64_t p) {
+    if (WIDE) { pair_io<VW>::ld_na(a, o, p); return; }
+    uint32_t x[VW], y[VW];
+    hint<VW>::ld_na(a, x, p); hint<VW>::ld_na(a + W, y, p); cat(o, x, y);
+  }
+  static __device__ __forceinline__ void st(uint32_t *a, uint32_t W, const uint32_t (&o)[N], uint64_t p) {
+    if (WIDE) { pair_io<VW>::st(a, o, p); return; }
+    uint32_t x[VW], y[VW];
+    cut(o, x, y); hint<VW>::st(a, x, p); hint<VW>::st(a + W, y, p);
+  }
+};
+
 /* Half-sweep of colour p.  One thread owns two adjacent columns (x/2 = 2j,
  * 2j+1; y) of one sample, VW replica words each (group grp of G = W/VW), and
  * marches over the z chunk [z0, z0 + zc).  The two sites share their row
@@ -224,13 +261,14 @@ __device__ __forceinline__ uint32_t ld_u16_keep(const uint8_t *a, uint64_t pol) 
  * bytes and the two demon words per plane.  Block = (TX pairs along x/2) x
  * (TY rows); TX divides L/4; grid = (L/4/TX, ytiles*ns*G, L/zc).
  * In-plane offsets are 32-bit (P*W < 2^32 is checked at creation). */
-template <int VW, bool MICSA>
+template <int VW, bool MICSA, bool WIDE>
 __global__ void __launch_bounds__(TPB)
 k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
         const int zc, const int pd, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
         uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
         const int *__restrict__ walk, const uint32_t *__restrict__ rnd) {
   constexpr int N = 2 * VW; /* words per pair */
+  using PR = pairs<VW, WIDE>;
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
   const uint32_t by = blockIdx.y;
   const uint32_t tile = by % ytiles, sg = by / ytiles; /* block-uniform */
@@ -285,8 +323,8 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
 
   /* other colour at (2j, 2j+1; y) for planes z0-1 and z0 */
   uint32_t vm[N], v0[N];
-  pair_io<VW>::ld_nc(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, vm, keep);
-  pair_io<VW>::ld_nc(oth + (z0 * plane + row) * W, v0, keep);
+  PR::ld_nc(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, W, vm, keep);
+  PR::ld_nc(oth + (z0 * plane + row) * W, W, v0, keep);
 
   uint32_t zdd = zd;
 #pragma unroll 2
@@ -295,17 +333,17 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
     const uint32_t zo = z * plane;
     const uint32_t rowoff = (y + z + p) & 1; /* x = 2*(x/2) + rowoff for both */
     uint32_t own[N], up[N], vn[N], vs[N], ext[VW], a0[N], a1[N], a2[N];
-    pair_io<VW>::ld(mine + (zo + row) * W, own, keep);
-    pair_io<VW>::ld_nc(oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, up, keep);
-    pair_io<VW>::ld_nc(oth + (zo + rowN) * W, vn, keep);
-    pair_io<VW>::ld_nc(oth + (zo + rowS) * W, vs, keep);
+    PR::ld(mine + (zo + row) * W, W, own, keep);
+    PR::ld_nc(oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, W, up, keep);
+    PR::ld_nc(oth + (zo + rowN) * W, W, vn, keep);
+    PR::ld_nc(oth + (zo + rowS) * W, W, vs, keep);
     hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
     const uint32_t jb2 = ld_u16_keep(jbp + zo + row, keep);
     if (MICSA) {
       const uint32_t sa = (zdd * plane + drowA) * W;
       if (dpair) {
-        pair_io<VW>::ld_na(q0b + sa, a0, strm);
-        pair_io<VW>::ld_na(q1b + sa, a1, strm);
+        PR::ld_na(q0b + sa, W, a0, strm);
+        PR::ld_na(q1b + sa, W, a1, strm);
       } else {
         const uint32_t sb = (zdd * plane + drowB) * W;
         uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
@@ -327,9 +365,9 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
       }
     } else {
       const uint32_t *rb = rnd + (size_t)(zo + row) * W + grp * VW;
-      pair_io<VW>::ld_na(rb, a0, strm);
-      pair_io<VW>::ld_na(rb + P * W, a1, strm);
-      pair_io<VW>::ld_na(rb + 2 * P * W, a2, strm);
+      PR::ld_na(rb, W, a0, strm);
+      PR::ld_na(rb + P * W, W, a1, strm);
+      PR::ld_na(rb + 2 * P * W, W, a2, strm);
     }
     /* x-neighbours: site A (x/2 = 2j) and B (2j+1) of colour p see, in the
      * other colour, +x at x/2 + rowoff and -x at x/2 + rowoff - 1 */
@@ -359,12 +397,12 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
         own[o] = sw ^ flip;
       }
     }
-    pair_io<VW>::st(mine + (zo + row) * W, own, keep);
+    PR::st(mine + (zo + row) * W, W, own, keep);
     if (MICSA) {
       const uint32_t sa = (zdd * plane + drowA) * W;
       if (dpair) {
-        pair_io<VW>::st(q0b + sa, a0, strm);
-        pair_io<VW>::st(q1b + sa, a1, strm);
+        PR::st(q0b + sa, W, a0, strm);
+        PR::st(q1b + sa, W, a1, strm);
       } else {
         const uint32_t sb = (zdd * plane + drowB) * W;
         uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
@@ -663,10 +701,17 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
   const int zc = g.zc > 0 ? g.zc : ((g.L >= 128 && g.L % 16 == 0) ? 16 : (g.L >= 48 ? 8 : 2));
   dim3 block(tx, ty);
   dim3 grid(g.Lh / 2 / tx, ytiles * g.ns * G, g.L / zc);
-  if (micsa)
-    k_sweep<VW, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
-  else
-    k_sweep<VW, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
+  if (G == 1) {
+    if (micsa)
+      k_sweep<VW, true, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
+    else
+      k_sweep<VW, false, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
+  } else {
+    if (micsa)
+      k_sweep<VW, true, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
+    else
+      k_sweep<VW, false, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
+  }
   return cudaGetLastError();
 }
 
