@@ -118,6 +118,30 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
  * The reference has fixed launch geometry (calculate_blocks, ini.c:580-602). */
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n);
 
+/* Spin energies computed without allocating any device memory; this entry
+ * point has no counterpart in the reference.  It is for callers that cannot
+ * call cudaMalloc when they measure: processes that size their device memory
+ * once at start-up (services, real-time loops), whose device memory belongs
+ * to another allocator, or that must not let an allocation synchronise their
+ * streams.  The caller passes device pointers to the reference's own
+ * device-resident words of nsamples samples, concatenated by sample:
+ *   even, odd  [s][H][nr] uint64   (d_spin, CopyDataOnDevice main.cu:429-434)
+ *   J          [s][12][H] uint64   (d_J,    CopyDataOnDevice main.cu:436-455)
+ * and a device int32 output e_spin[s*nr + r] (h_Ener of Measure_Energy_Spins).
+ * Work is queued on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * The per-replica counters live in one fixed device array of
+ * MICSA_NOALLOC_MAX_REPLICAS entries per GPU, kept until the process exits:
+ * nr * nsamples above that limit is rejected with MICSA_ERR_ARG.  Every call
+ * shares the array (each call zeroes the part it uses), so calls that overlap
+ * on the GPU race: keep them in one stream or otherwise ordered.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress
+ * on the current device); make that first call before any stream capture.
+ * err (optional) receives a message on failure. */
+#define MICSA_NOALLOC_MAX_REPLICAS 8192
+int micsa_energy_noalloc(int L, int nr, int nsamples, const uint64_t *even, const uint64_t *odd,
+                         const uint64_t *J, int32_t *e_spin, void *stream, char *err,
+                         size_t errlen);
+
 /* Wait for all work issued on the context (cudaDeviceSynchronize,
  * main.cu:144,149) and report any asynchronous error. */
 int micsa_synchronize(micsa_ctx *ctx);

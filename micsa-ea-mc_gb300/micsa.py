@@ -21,9 +21,10 @@ ABI_SYMBOLS = [
     "micsa_create", "micsa_destroy", "micsa_last_error", "micsa_footprint_bytes",
     "micsa_set_lut", "micsa_upload_couplings", "micsa_upload_spins", "micsa_upload_demons",
     "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
-    "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_synchronize",
-    "micsa_kernel_launches", "micsa_stream",
+    "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_energy_noalloc",
+    "micsa_synchronize", "micsa_kernel_launches", "micsa_stream",
 ]
+NOALLOC_MAX_REPLICAS = 8192
 
 _lib = None
 
@@ -85,6 +86,9 @@ def lib():
         "micsa_profile": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double),
                                     C.POINTER(C.c_double)]),
         "micsa_tuning_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+        "micsa_energy_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
+                                           C.c_size_t]),
         "micsa_synchronize": (C.c_int, [C.c_void_p]),
         "micsa_kernel_launches": (C.c_int64, [C.c_void_p]),
         "micsa_stream": (C.c_void_p, [C.c_void_p]),
