@@ -76,6 +76,22 @@ int micsa_upload_spins(micsa_ctx *ctx, int sample, const uint64_t *even,
 int micsa_upload_demons(micsa_ctx *ctx, int sample, const uint64_t *w0,
                         const uint64_t *w1);
 
+/* One demon refresh drawn on the GPU: InitWalkers (ini.c:712-781) for the nr
+ * replica streams of samples first .. first+count-1, written straight into
+ * the device demons (the upload of refresh_walkers, main.cu:340-366), each
+ * sample's demon walk reset.  prc and xo are those samples' streams,
+ * [count][nr] of the reference's s_aleatorio_HQ_64bits (2080 bytes) and
+ * s_xoshiro256pp (48 bytes, random_generator.h:28-44), in the state
+ * InitWalkers would start from; on return they hold, byte for byte, the
+ * state it leaves.  thr are get_thresholds' three thresholds
+ * (ini.c:680-710).  Every demon equals the reference's draw: each stream is
+ * cut into segments whose start states are reached by jump-ahead.  The
+ * device work is queued on the context's stream; the call returns once the
+ * caller's structs are advanced.  No counterpart in the reference, which
+ * draws on host threads. */
+int micsa_refresh_demons(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
+                         const uint64_t *thr);
+
 /* One iteration of Monte_Carlo (main.cu:197-313) on all samples.
  *   flag = 1: nc x (even, odd) microcanonical half-sweeps, then the demon
  *             walk.  te and keys are ignored (may be NULL).

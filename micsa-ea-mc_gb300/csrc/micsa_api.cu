@@ -12,9 +12,11 @@
 #include <string.h>
 
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "micsa.h"
+#include "micsa_jump.h"
 #include "micsa_kernels.cuh"
 
 #define MICSA_TUNE_MAX 24
@@ -38,6 +40,11 @@ struct micsa_ctx {
   int ntune = 0;           /* launch shapes timed at creation */
   int tune_zc[MICSA_TUNE_MAX] = {0}, tune_pd[MICSA_TUNE_MAX] = {0};
   double tune_ms[MICSA_TUNE_MAX] = {0};
+  /* demon refresh on the device: jump tables of one segment length */
+  micsa_refresh_plan plan = {};
+  uint64_t *plan_lcg = nullptr, *plan_xo = nullptr, *plan_fib = nullptr;
+  uint64_t *rec = nullptr;
+  size_t rec_words = 0;
   char err[512] = {0};
 };
 
@@ -299,11 +306,13 @@ int micsa_destroy(micsa_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
-  void *bufs[] = {ctx->spin, ctx->dem0, ctx->dem1, ctx->rnd, ctx->jb, ctx->lut,
-                  ctx->te,   ctx->keys, ctx->walk, ctx->stage, ctx->acc};
+  void *bufs[] = {ctx->spin, ctx->dem0,     ctx->dem1,    ctx->rnd,      ctx->jb,
+                  ctx->lut,  ctx->te,       ctx->keys,    ctx->walk,     ctx->stage,
+                  ctx->acc,  ctx->plan_lcg, ctx->plan_xo, ctx->plan_fib, ctx->rec};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  micsa_refresh_plan_free(&ctx->plan);
   delete ctx;
   return MICSA_OK;
 }
@@ -410,6 +419,98 @@ int micsa_upload_demons(micsa_ctx *ctx, int sample, const uint64_t *w0, const ui
   MICSA_CK(cudaMemsetAsync(ctx->walk + sample, 0, sizeof(int), ctx->stream));
   MICSA_CK(cudaStreamSynchronize(ctx->stream));
   ctx->have_dem[sample] = 1;
+  return MICSA_OK;
+}
+
+namespace {
+
+/* jump tables for segments of wps words, on the host and the device */
+int ensure_refresh_plan(micsa_ctx *ctx, int64_t nw, int wps) {
+  if (ctx->plan.lcg && ctx->plan.nwords == nw && ctx->plan.words_per_seg == wps) return MICSA_OK;
+  MICSA_CK(cudaStreamSynchronize(ctx->stream)); /* the old tables may still be read */
+  micsa_refresh_plan_free(&ctx->plan);
+  for (uint64_t **b : {&ctx->plan_lcg, &ctx->plan_xo, &ctx->plan_fib}) {
+    if (*b) cudaFree(*b);
+    *b = nullptr;
+  }
+  if (micsa_refresh_plan_make(nw, wps, &ctx->plan))
+    return fail(ctx, MICSA_ERR_NOMEM, "refresh jump tables (%lld words, %d per segment)",
+                (long long)nw, wps);
+  const int64_t ns = ctx->plan.nseg;
+  MICSA_CK(cudaMalloc(&ctx->plan_lcg, 2 * ns * sizeof(uint64_t)));
+  MICSA_CK(cudaMalloc(&ctx->plan_xo, 4 * ns * sizeof(uint64_t)));
+  MICSA_CK(cudaMalloc(&ctx->plan_fib, MICSA_FIB_R * ns * sizeof(uint64_t)));
+  MICSA_CK(cudaMemcpy(ctx->plan_lcg, ctx->plan.lcg, 2 * ns * 8, cudaMemcpyHostToDevice));
+  MICSA_CK(cudaMemcpy(ctx->plan_xo, ctx->plan.xo, 4 * ns * 8, cudaMemcpyHostToDevice));
+  MICSA_CK(cudaMemcpy(ctx->plan_fib, ctx->plan.fib, MICSA_FIB_R * ns * 8, cudaMemcpyHostToDevice));
+  return MICSA_OK;
+}
+
+}  // namespace
+
+int micsa_refresh_demons(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
+                         const uint64_t *thr) {
+  if (!ctx || !prc || !xo || !thr) return fail(ctx, MICSA_ERR_ARG, "null argument");
+  if (first < 0 || count < 1 || first + count > ctx->cfg.nsamples)
+    return fail(ctx, MICSA_ERR_ARG, "samples [%d, %d) out of range [0, %d)", first, first + count,
+                ctx->cfg.nsamples);
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  const micsa_geo &g = ctx->g;
+  micsa_prc_t *P = (micsa_prc_t *)prc;
+  micsa_xoshiro_t *X = (micsa_xoshiro_t *)xo;
+  const int64_t nw = 2 * g.H * g.nc, nstreams = (int64_t)count * g.nr;
+  /* segments of 32 words (2048 draws), shorter when the call has few warps */
+  int wps = 32;
+  while (wps > 2 && (int64_t)count * g.W * ((nw + wps - 1) / wps) < 4096) wps >>= 1;
+
+  /* start records, grouped by warp; checked before anything changes */
+  std::vector<uint64_t> rec((size_t)nstreams * MICSA_STREAM_REC);
+  uint64_t one[MICSA_STREAM_REC];
+  for (int64_t s = 0; s < nstreams; s++) {
+    if (micsa_stream_record(&P[s], &X[s], one))
+      return fail(ctx, MICSA_ERR_ARG, "stream %lld: PR ring pointers are not 24, 55, 61 apart",
+                  (long long)s);
+    const int64_t grp = s / 32, lane = s % 32;
+    for (int k = 0; k < MICSA_STREAM_REC; k++) rec[(grp * MICSA_STREAM_REC + k) * 32 + lane] = one[k];
+  }
+  if ((rc = ensure_refresh_plan(ctx, nw, wps))) return rc;
+  if (ctx->rec_words < rec.size()) {
+    MICSA_CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->rec) cudaFree(ctx->rec);
+    ctx->rec = nullptr;
+    MICSA_CK(cudaMalloc(&ctx->rec, rec.size() * sizeof(uint64_t)));
+    ctx->rec_words = rec.size();
+  }
+  /* pageable source: the call returns once the words are staged */
+  MICSA_CK(cudaMemcpyAsync(ctx->rec, rec.data(), rec.size() * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice, ctx->stream));
+  MICSA_CK(micsa_launch_refresh(g, first, count, nw, wps, ctx->plan.nseg, ctx->rec, ctx->plan_lcg,
+                                ctx->plan_xo, ctx->plan_fib, thr, ctx->dem0, ctx->dem1,
+                                ctx->stream));
+  ctx->launches++;
+  MICSA_CK(cudaMemsetAsync(ctx->walk + first, 0, count * sizeof(int), ctx->stream));
+
+  /* the caller's streams move past the draws while the device makes them */
+  const micsa_refresh_plan *plan = &ctx->plan;
+  auto advance = [=](int64_t s0, int64_t s1) {
+    for (int64_t s = s0; s < s1; s++) micsa_streams_advance_plan(plan, &P[s], &X[s]);
+  };
+  unsigned hw = std::thread::hardware_concurrency();
+  int64_t nt = nstreams / 64;
+  if (nt > (int64_t)hw) nt = hw;
+  if (nt < 1) nt = 1;
+  std::vector<std::thread> pool;
+  for (int64_t t = 1; t < nt; t++) {
+    try {
+      pool.emplace_back(advance, nstreams * t / nt, nstreams * (t + 1) / nt);
+    } catch (...) {
+      advance(nstreams * t / nt, nstreams * (t + 1) / nt);
+    }
+  }
+  advance(0, nstreams / nt);
+  for (auto &th : pool) th.join();
+  for (int s = first; s < first + count; s++) ctx->have_dem[s] = 1;
   return MICSA_OK;
 }
 

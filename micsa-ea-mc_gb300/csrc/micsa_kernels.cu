@@ -795,3 +795,122 @@ int micsa_sweep_zc_candidates(int L, int *out, int max) {
     if (L % zc == 0) out[n++] = zc;
   return n;
 }
+
+/* ------------------------------------------------------- demon refresh */
+/* One refresh (InitWalkers, ini.c:712-781) drawn on the device.  A warp
+ * owns 32 replica streams (w*32 + lane) of one sample and one segment of
+ * wps CPUwalker words; rec holds each stream's start state grouped by warp,
+ * rec[(grp*REFRESH_REC + k)*32 + lane], grp = j*W + w (layout of
+ * micsa_stream_record).  The lane jumps its generators to draw m = seg*64*wps:
+ *   lagged Fibonacci  x_{m-61+t} = sum_i fib[i] E[i+t] for t < 55, then the
+ *                     recurrence gives x_{m-6} .. x_{m-1};
+ *   congruential      z -> lcg[0] z + lcg[1];
+ *   xoshiro           s -> q(T) s = sum of T^i s over the bits i of q.
+ * Each word is then 64 draws with the PR ring in registers (ring slot = draw
+ * index mod 64, constant after unrolling), and four warp transposes turn the
+ * 32 streams' words into device words of the sites (walk translation 0). */
+constexpr int REFRESH_REC = 120;
+constexpr uint64_t REFRESH_LCG_A = 3202034522624059733ULL; /* random_generator.h:66 */
+
+__device__ __forceinline__ uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+__device__ __forceinline__ void xoshiro_step(uint64_t &s0, uint64_t &s1, uint64_t &s2,
+                                             uint64_t &s3) {
+  const uint64_t t = s1 << 17;
+  s2 ^= s0;
+  s3 ^= s1;
+  s1 ^= s2;
+  s0 ^= s3;
+  s2 ^= t;
+  s3 = rotl64(s3, 45);
+}
+
+__global__ void __launch_bounds__(64)
+k_refresh(const micsa_geo g, const int first, const int count, const int64_t nwords,
+          const int wps, const int64_t nseg, const uint64_t *__restrict__ rec,
+          const uint64_t *__restrict__ lcg, const uint64_t *__restrict__ xoq,
+          const uint64_t *__restrict__ fib, const uint64_t t0, const uint64_t t1,
+          const uint64_t t2, uint32_t *__restrict__ dem0, uint32_t *__restrict__ dem1) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (warp >= (int64_t)count * g.W * nseg) return; /* whole warps only */
+  const int64_t seg = warp % nseg, grp = warp / nseg;
+  const int w = (int)(grp % g.W), j = (int)(grp / g.W);
+  const uint64_t *R = rec + grp * REFRESH_REC * 32 + lane;
+
+  uint64_t ring[64];
+  if (seg == 0) {
+#pragma unroll
+    for (int t = 0; t < 61; t++) ring[3 + t] = R[t * 32];
+  } else {
+#pragma unroll
+    for (int t = 0; t < 55; t++) ring[3 + t] = 0;
+    const uint64_t *c = fib + seg * 55;
+    const uint64_t *E = R + 6 * 32;
+    for (int i = 0; i < 55; i++) {
+      const uint64_t ci = c[i];
+#pragma unroll
+      for (int t = 0; t < 55; t++) ring[3 + t] += ci * E[(i + t) * 32];
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) ring[58 + k] = ring[34 + k] + ring[3 + k];
+  }
+  uint64_t z = lcg[2 * seg] * R[115 * 32] + lcg[2 * seg + 1];
+  uint64_t s0 = R[116 * 32], s1 = R[117 * 32], s2 = R[118 * 32], s3 = R[119 * 32];
+  if (seg != 0) {
+    uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    for (int qw = 0; qw < 4; qw++) {
+      uint64_t bits = xoq[4 * seg + qw];
+      for (int b = 0; b < 64; b++, bits >>= 1) {
+        if (bits & 1) { a0 ^= s0; a1 ^= s1; a2 ^= s2; a3 ^= s3; }
+        xoshiro_step(s0, s1, s2, s3);
+      }
+    }
+    s0 = a0; s1 = a1; s2 = a2; s3 = a3;
+  }
+
+  const int64_t i0 = seg * wps;
+  const int64_t i1 = i0 + wps < nwords ? i0 + wps : nwords;
+  const int sample = first + j;
+  for (int64_t i = i0; i < i1; i++) {
+    uint64_t d0 = 0, d1 = 0;
+#pragma unroll
+    for (int b = 0; b < 64; b++) {
+      const uint64_t xo_out = rotl64(s0 + s3, 23) + s0;
+      xoshiro_step(s0, s1, s2, s3);
+      const uint64_t xn = ring[(b - 24) & 63] + ring[(b - 55) & 63];
+      const uint64_t pr = xn ^ ring[(b - 61) & 63];
+      ring[b] = xn;
+      z = z * REFRESH_LCG_A + 1;
+      const uint64_t e = (z + pr) + xo_out;
+      const uint32_t a0 = e < t0, a1 = e < t1, a2 = e < t2;
+      d0 |= (uint64_t)(a0 ^ a1 ^ a2) << b;
+      d1 |= (uint64_t)((a0 & a1) | (a0 & a2) | (a1 & a2)) << b;
+    }
+    const int64_t pi = i / g.H, h = i % g.H;
+    const int p = (int)(pi / g.nc), ic = (int)(pi % g.nc);
+    const uint32_t lo0 = warp_transpose32((uint32_t)d0, lane);
+    const uint32_t hi0 = warp_transpose32((uint32_t)(d0 >> 32), lane);
+    const uint32_t lo1 = warp_transpose32((uint32_t)d1, lane);
+    const uint32_t hi1 = warp_transpose32((uint32_t)(d1 >> 32), lane);
+    const site_xyz sa = ref_site(g, p, h, lane), sb = ref_site(g, p, h, lane + 32);
+    const int64_t base = ((int64_t)sample * 2 * g.nc + pi) * g.P * g.W + w;
+    const int64_t oa = base + demon_slot(g, p, ic, 0, sa.x, sa.y, sa.z) * g.W;
+    const int64_t ob = base + demon_slot(g, p, ic, 0, sb.x, sb.y, sb.z) * g.W;
+    dem0[oa] = lo0;
+    dem0[ob] = hi0;
+    dem1[oa] = lo1;
+    dem1[ob] = hi1;
+  }
+}
+
+cudaError_t micsa_launch_refresh(const micsa_geo &g, int first, int count, int64_t nwords,
+                                 int wps, int64_t nseg, const uint64_t *rec, const uint64_t *lcg,
+                                 const uint64_t *xoq, const uint64_t *fib, const uint64_t thr[3],
+                                 uint32_t *dem0, uint32_t *dem1, cudaStream_t st) {
+  const int64_t warps = (int64_t)count * g.W * nseg;
+  k_refresh<<<(unsigned)((warps + 1) / 2), 64, 0, st>>>(g, first, count, nwords, wps, nseg, rec,
+                                                        lcg, xoq, fib, thr[0], thr[1], thr[2],
+                                                        dem0, dem1);
+  return cudaGetLastError();
+}

@@ -75,4 +75,14 @@ cudaError_t micsa_launch_overlap(const micsa_geo &g, const uint32_t *spin,
                                  unsigned long long *qd, unsigned long long *c4d,
                                  cudaStream_t st);
 
+/* One demon refresh of samples first .. first+count-1 drawn from the
+ * streams' start records rec (grouped by warp, 120 words per stream) and
+ * the segment jump tables lcg/xoq/fib of wps words per segment; writes
+ * every demon word of those samples with walk translation 0. */
+cudaError_t micsa_launch_refresh(const micsa_geo &g, int first, int count, int64_t nwords,
+                                 int wps, int64_t nseg, const uint64_t *rec,
+                                 const uint64_t *lcg, const uint64_t *xoq,
+                                 const uint64_t *fib, const uint64_t thr[3],
+                                 uint32_t *dem0, uint32_t *dem1, cudaStream_t st);
+
 #endif

@@ -145,6 +145,7 @@ typedef struct {
   int32_t *e_spin;
   uint64_t *e_demon;
   int nthreads;
+  int gpu_refresh; /* demon refresh on the GPU (default) or on host threads */
 } model_t;
 
 static model_t M;
@@ -617,8 +618,35 @@ static void *refresh_worker(void *arg) {
   return NULL;
 }
 
+/* refresh_walkers (main.cu:340-377) with the draws on the GPU: the walkers
+ * the reference would upload now are the next draws of each stream, so they
+ * are drawn now, on the device, from the streams' current state; the
+ * snapshot written with the next checkpoint is the state after them, as in
+ * the reference.  A resumed run first uploads the walkers of its checkpoint. */
+static void refresh_walkers_gpu(micsa_ctx *ctx, int *first) {
+  for (int b = 0; b < M.nbits; b++) {
+    if (!(*first * data.flag)) {
+      int rc;
+      if (*first) {
+        rc = micsa_upload_demons(ctx, b, M.w0[b], M.w1[b]);
+      } else {
+        rc = micsa_refresh_demons(ctx, b, 1, M.random_PRC_C[b], M.random_xo_C[b], M.thr);
+      }
+      if (rc) die("demon refresh: %s\n", micsa_last_error(ctx));
+      memcpy(M.write_PRC_C[b], M.random_PRC_C[b], sizeof(micsa_prc_t) * M.nr);
+      memcpy(M.write_xo_C[b], M.random_xo_C[b], sizeof(micsa_xoshiro_t) * M.nr);
+    }
+    M.icds[b].first = 0; /* InitWalkers, ini.c:739-741 */
+  }
+  *first = 0;
+}
+
 /* refresh_walkers (main.cu:340-377) */
 static void refresh_walkers(micsa_ctx *ctx, int *first) {
+  if (M.gpu_refresh) {
+    refresh_walkers_gpu(ctx, first);
+    return;
+  }
   if (!(*first * data.flag)) {
     if (!*first && R.running) {
       pthread_join(R.tid, NULL);
@@ -729,6 +757,8 @@ int main(int argc, char **argv) {
     const char *nt = getenv("MICSA_HOST_THREADS");
     long cores = sysconf(_SC_NPROCESSORS_ONLN);
     M.nthreads = nt ? atoi(nt) : (int)(cores > 1 ? cores : 1);
+    const char *where = getenv("MICSA_REFRESH");
+    M.gpu_refresh = !(where && !strcmp(where, "host"));
   }
   create_sample_path(sample);
   int write_seeds = check_and_prepare();

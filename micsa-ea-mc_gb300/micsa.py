@@ -20,7 +20,7 @@ STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE", 
 ABI_SYMBOLS = [
     "micsa_create", "micsa_destroy", "micsa_last_error", "micsa_footprint_bytes",
     "micsa_set_lut", "micsa_upload_couplings", "micsa_upload_spins", "micsa_upload_demons",
-    "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
+    "micsa_refresh_demons", "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
     "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_energy_noalloc",
     "micsa_synchronize", "micsa_kernel_launches", "micsa_stream",
 ]
@@ -48,6 +48,17 @@ class PRC(C.Structure):
 class Xoshiro(C.Structure):
     """micsa_xoshiro_t: the reference's s_xoshiro256pp (48 bytes)."""
     _fields_ = [("s", C.c_uint64 * 4), ("t", C.c_uint64), ("out", C.c_uint64)]
+
+
+class RefreshPlan(C.Structure):
+    """micsa_refresh_plan (host/micsa_jump.h): jump tables of one refresh shape."""
+    _fields_ = [("nwords", C.c_int64), ("words_per_seg", C.c_int64), ("nseg", C.c_int64),
+                ("lcg", C.POINTER(C.c_uint64)), ("xo", C.POINTER(C.c_uint64)),
+                ("fib", C.POINTER(C.c_uint64)), ("adv_lcg", C.c_uint64 * 2),
+                ("adv_xo", C.c_uint64 * 4), ("adv_fib", C.c_uint64 * 55)]
+
+
+STREAM_REC = 120  # words of one stream's start record (micsa_stream_record)
 
 
 def _ptr(a, ctype):
@@ -78,6 +89,8 @@ def lib():
         "micsa_upload_couplings": (C.c_int, [C.c_void_p, C.c_int, u64p]),
         "micsa_upload_spins": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
         "micsa_upload_demons": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
+        "micsa_refresh_demons": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(PRC),
+                                           C.POINTER(Xoshiro), u64p]),
         "micsa_monte_carlo": (C.c_int, [C.c_void_p, C.c_int, u32p, u32p]),
         "micsa_iterate": (C.c_int, [C.c_void_p, C.c_int64]),
         "micsa_measure": (C.c_int, [C.c_void_p, i32p, u64p, i64p, i64p]),
@@ -108,6 +121,22 @@ def lib():
                                             C.c_int, C.c_int, u64p, u64p, C.c_int]),
         "micsa_fill_bits": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), C.c_int, C.c_uint64,
                                    C.c_int, C.c_uint32, u32p]),
+        "micsa_draw_demons": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), u64p, C.c_int, C.c_int,
+                                     C.c_int, C.c_int, u64p, u64p]),
+        # jump-ahead of the refresh streams (micsa-ea-mc_gb300/host/micsa_jump.h)
+        "micsa_lcg_jump": (None, [C.c_uint64, u64p, u64p]),
+        "micsa_fib_jump": (None, [C.c_uint64, u64p]),
+        "micsa_xoshiro_charpoly": (None, [u64p]),
+        "micsa_xoshiro_jump_poly": (None, [C.c_uint64, u64p]),
+        "micsa_xoshiro_apply": (None, [u64p, u64p]),
+        "micsa_streams_advance": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), C.c_uint64]),
+        "micsa_refresh_plan_make": (C.c_int, [C.c_int64, C.c_int64, C.POINTER(RefreshPlan)]),
+        "micsa_refresh_plan_free": (None, [C.POINTER(RefreshPlan)]),
+        "micsa_stream_record": (C.c_int, [C.POINTER(PRC), C.POINTER(Xoshiro), u64p]),
+        "micsa_streams_advance_plan": (None, [C.POINTER(RefreshPlan), C.POINTER(PRC),
+                                              C.POINTER(Xoshiro)]),
+        "micsa_draw_segment": (None, [C.POINTER(RefreshPlan), C.c_int64, u64p, u64p, C.c_int,
+                                      C.c_int, u64p, u64p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -172,6 +201,17 @@ class Context:
         b = np.ascontiguousarray(w1, dtype=np.uint64)
         check(self.h, lib().micsa_upload_demons(self.h, s, _ptr(a, C.c_uint64), _ptr(b, C.c_uint64)),
               "upload_demons")
+
+    def refresh_demons(self, first, prc, xo, thr):
+        """Demon refresh on the GPU for samples first .. first+len(prc)/nr-1;
+        prc/xo (ctypes arrays of PRC / Xoshiro, [count][nr]) are advanced in
+        place as InitWalkers would advance them."""
+        count, rem = divmod(len(prc), self.nr)
+        if rem or len(xo) != len(prc):
+            raise ValueError("need count*nr streams of each generator")
+        t = np.ascontiguousarray(thr, dtype=np.uint64)
+        check(self.h, lib().micsa_refresh_demons(self.h, first, count, prc, xo, _ptr(t, C.c_uint64)),
+              "refresh_demons")
 
     def monte_carlo(self, flag, te=None, keys=None):
         t = None if te is None else np.ascontiguousarray(te, dtype=np.uint32)

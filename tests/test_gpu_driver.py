@@ -28,7 +28,19 @@ def test_driver_matches_reference_files(golden, workdir):
     assert "finished at iteration" in out
 
 
-def test_driver_resume_is_bit_exact(workdir):
+@pytest.mark.parametrize("name", ["L16_NR64_2s_nc6", "L8_NR64_2s_nc3_therm"])
+def test_driver_host_refresh_matches_reference_files(name, workdir):
+    """MICSA_REFRESH=host: demons drawn on host threads while the GPU sweeps,
+    as the reference does, instead of on the GPU."""
+    import json
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", name + ".json")))
+    env = dict(os.environ, MICSA_REFRESH="host")
+    got, _ = runs.run_program(micsa.DRIVER_PATH, g["cfg"], workdir, env=env)
+    runs.compare(got, g, "micsa_run (host refresh) %s" % name)
+
+
+@pytest.mark.parametrize("refresh", ["gpu", "host"])
+def test_driver_resume_is_bit_exact(workdir, refresh):
     """Stop at an intermediate measurement (maxtime), resume with flag 0 from
     the conf/walkers checkpoints, and end where an uninterrupted run ends.
     (A case without thermalisation: the reference re-runs its nterm
@@ -38,8 +50,9 @@ def test_driver_resume_is_bit_exact(workdir):
     g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "L16_NR64_2s_nc6.json")))
     cfg = dict(g["cfg"])
     assert cfg["nterm"] == 0
-    runs.run_program(micsa.DRIVER_PATH, dict(cfg, maxtime=16), workdir)
-    got, _ = runs.run_program(micsa.DRIVER_PATH, dict(cfg, flag=0), workdir)
+    env = dict(os.environ, MICSA_REFRESH=refresh)
+    runs.run_program(micsa.DRIVER_PATH, dict(cfg, maxtime=16), workdir, env=env)
+    got, _ = runs.run_program(micsa.DRIVER_PATH, dict(cfg, flag=0), workdir, env=env)
     for t in ("32", "64", "128"):
         for b in ("0", "1"):
             assert got["times"][t][b]["spins"] == g["times"][t][b]["spins"]
