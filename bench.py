@@ -228,43 +228,116 @@ def run_micsa(a, dist):
             "launch_ms": round(sweep_ms, 5), "iteration_ms_profiled": round(iter_ms, 5),
             "autotune": ctx.tuning(),
             "traffic": traffic, "traffic_source": tnote}
-    # ---- end to end through the C ABI with host buffers: every step uploads
-    # the demon refresh set from pinned memory (refresh_walkers), runs the
-    # iteration and reads the energies back (Measure_Energy_Spins + demons)
+    # ---- end to end through the C ABI with host buffers
     e2e = None
     if not a.no_e2e:
-        pinned = []
-        for b in range(ns):
-            pair = []
-            for w in demons[b]:
-                t = torch.empty(w.size, dtype=torch.int64, pin_memory=True)
-                arr = t.numpy().view(np.uint64)
-                arr[:] = w
-                pair.append((t, arr))
-            pinned.append(pair)
-        h2d = sum(p[1].nbytes for pair in pinned for p in pair)
-        d2h = ns * nr * (4 + 8)
-        for _ in range(max(1, a.warmup)):
-            for b in range(ns):
-                ctx.upload_demons(b, pinned[b][0][1], pinned[b][1][1])
-            ctx.iterate(1)
-            ctx.measure(spin=True, demon=True)
-        ke = max(3, a.steps // 2)
-        dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            for b in range(ns):
-                ctx.upload_demons(b, pinned[b][0][1], pinned[b][1][1])
-            ctx.iterate(1)
-            ctx.measure(spin=True, demon=True)
-        te = dist.max((time.perf_counter() - t0) / ke)
-        e2e = {"value": round(attempts * dist.world / (te * 1e12), 4), "unit": UNIT,
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "ms_per_step": round(te * 1e3, 4), "steps": ke,
-               "step": "upload demon refresh set (pinned host) + 1 iteration + energy readback"}
+        e2e = e2e_job(a, dist, ctx, hm, attempts)
+        e2e["upload_every_step"] = e2e_upload_every_step(a, dist, ctx, demons, attempts)
     ctx.close()
     return dict(value=value, ms=ms, roof=roof, clocks=ck, e2e=e2e, launches=launches,
                 attempts=attempts)
+
+
+def _pinned(arr):
+    import torch
+    t = torch.empty(arr.size * arr.itemsize // 8, dtype=torch.int64, pin_memory=True)
+    v = t.numpy().view(arr.dtype)
+    v[:] = arr
+    return t, v
+
+
+def e2e_job(a, dist, ctx, hm, attempts):
+    """The whole job of `steps` iterations through the C ABI, on the
+    reference's schedule (main.cu:126-180): start state uploaded from pinned
+    host memory, demon refresh and energy readback at t = 0, 1, 2, 4, ...
+    (refresh_walkers + Measure_Energy_Spins/Clerics), iterations in between,
+    and the final spins and demons read back (the checkpoint of
+    copy_from_GPU_for_write).  h2d/d2h are the bytes of those copies per
+    iteration."""
+    import micsa
+    L, nr, ns, nc = a.L, a.nr, a.nsamples, a.nc
+    H = (L // 4) ** 3 // 2
+    J = [_pinned(hm.J[b]) for b in range(ns)]
+    sp = [(_pinned(hm.spins[b][0]), _pinned(hm.spins[b][1])) for b in range(ns)]
+    start = [(bytes(hm.prc_C[b]), bytes(hm.xo_C[b])) for b in range(ns)]
+    outs = [(_pinned(np.zeros(H * nr, np.uint64)), _pinned(np.zeros(H * nr, np.uint64)),
+             _pinned(np.zeros(2 * H * nc * nr, np.uint64)),
+             _pinned(np.zeros(2 * H * nc * nr, np.uint64))) for b in range(ns)]
+    p64 = lambda v: v.ctypes.data_as(micsa.C.POINTER(micsa.C.c_uint64))
+    lib = micsa.lib()
+
+    def job():
+        prc = [(micsa.PRC * nr).from_buffer_copy(start[b][0]) for b in range(ns)]
+        xo = [(micsa.Xoshiro * nr).from_buffer_copy(start[b][1]) for b in range(ns)]
+        for b in range(ns):
+            micsa.check(ctx.h, lib.micsa_upload_couplings(ctx.h, b, p64(J[b][1])), "couplings")
+            micsa.check(ctx.h, lib.micsa_upload_spins(ctx.h, b, p64(sp[b][0][1]), p64(sp[b][1][1])),
+                        "spins")
+        t, nref, nmeas = 0, 0, 0
+        while t < a.steps:
+            if t & (t - 1) == 0:
+                for b in range(ns):
+                    ctx.refresh_demons(b, prc[b], xo[b], hm.thr)
+                nref += 1
+            nxt = 1
+            while nxt <= t:
+                nxt <<= 1
+            nxt = min(nxt, a.steps)
+            ctx.iterate(nxt - t)
+            t = nxt
+            if t & (t - 1) == 0 or t == a.steps:
+                ctx.measure(spin=True, demon=True)
+                nmeas += 1
+        for b in range(ns):
+            o = outs[b]
+            micsa.check(ctx.h, lib.micsa_download_spins(ctx.h, b, p64(o[0][1]), p64(o[1][1])), "spins")
+            micsa.check(ctx.h, lib.micsa_download_demons(ctx.h, b, p64(o[2][1]), p64(o[3][1])),
+                        "demons")
+        return nref, nmeas
+
+    job()  # warm-up: jump tables, graph capture
+    ctx.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    nref, nmeas = job()
+    ctx.synchronize()
+    te = dist.max(time.perf_counter() - t0)
+    h2d = ns * (12 * H * 8 + 2 * H * nr * 8) + nref * ns * nr * 120 * 8
+    d2h = nmeas * ns * nr * (4 + 8) + ns * (2 * H * nr * 8 + 2 * 2 * H * nc * nr * 8)
+    return {"value": round(attempts * a.steps * dist.world / (te * 1e12), 4), "unit": UNIT,
+            "h2d_bytes_per_step": int(h2d // a.steps), "d2h_bytes_per_step": int(d2h // a.steps),
+            "ms_per_step": round(te * 1e3 / a.steps, 4), "job_ms": round(te * 1e3, 2),
+            "refreshes": nref, "measurements": nmeas,
+            "step": "job of `steps` iterations: state upload, GPU demon refresh + energy readback "
+                    "at t=0,1,2,4,..., final spins+demons readback"}
+
+
+def e2e_upload_every_step(a, dist, ctx, demons, attempts):
+    """Worst case: every iteration re-uploads the whole demon set from
+    pinned host memory (the reference's refresh upload, main.cu:355-362) and
+    reads the energies back."""
+    ns, nr = a.nsamples, a.nr
+    pinned = [(_pinned(demons[b][0]), _pinned(demons[b][1])) for b in range(ns)]
+    h2d = sum(p[1].nbytes for pair in pinned for p in pair)
+    d2h = ns * nr * (4 + 8)
+
+    def step():
+        for b in range(ns):
+            ctx.upload_demons(b, pinned[b][0][1], pinned[b][1][1])
+        ctx.iterate(1)
+        ctx.measure(spin=True, demon=True)
+
+    for _ in range(max(1, a.warmup)):
+        step()
+    ke = max(3, min(20, a.steps // 2))
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        step()
+    te = dist.max((time.perf_counter() - t0) / ke)
+    return {"value": round(attempts * dist.world / (te * 1e12), 4), "unit": UNIT,
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": round(te * 1e3, 4), "steps": ke}
 
 
 def cpu_state(L, nr, ns, nc, seed=7):

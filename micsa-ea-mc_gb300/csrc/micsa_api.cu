@@ -156,6 +156,22 @@ int autotune(micsa_ctx *ctx) {
   int zcs[8];
   const int nz = micsa_sweep_zc_candidates(g.L, zcs, 8);
   const int pds[3] = {0, 2, 4};
+  /* MICSA_SWEEP_ZC / MICSA_SWEEP_PD pin the shape and skip the timing
+   * (reproducible launch shapes, e.g. under a profiler, whose per-launch
+   * overhead would distort the choice) */
+  if (const char *ez = getenv("MICSA_SWEEP_ZC")) {
+    const char *ep = getenv("MICSA_SWEEP_PD");
+    const int zc = atoi(ez), pd = ep ? atoi(ep) : 0;
+    int ok = 0;
+    for (int c = 0; c < nz; c++) ok |= zcs[c] == zc;
+    if (!ok || (pd != 0 && pd != 2 && pd != 4) || (pd && pd >= zc))
+      return fail(ctx, MICSA_ERR_ARG, "MICSA_SWEEP_ZC=%d / MICSA_SWEEP_PD=%d not a shape for L=%d",
+                  zc, pd, g.L);
+    g.zc = zc;
+    g.pd = pd;
+    ctx->ntune = 0;
+    return MICSA_OK;
+  }
   cudaEvent_t e0, e1;
   MICSA_CK(cudaEventCreate(&e0));
   MICSA_CK(cudaEventCreate(&e1));
@@ -643,31 +659,29 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
   if (rc || (rc = ready_for_sweeps(ctx, 1))) return rc;
   const micsa_geo &g = ctx->g;
   const int per = 2 * g.nc;
-  std::vector<cudaEvent_t> ev((size_t)(n * (per + 1) + 1));
+  /* events around each iteration's half-sweeps (issued back to back, as in
+   * the graph) and around its walk */
+  std::vector<cudaEvent_t> ev((size_t)(2 * n + 1));
   for (auto &e : ev) MICSA_CK(cudaEventCreate(&e));
-  size_t k = 0;
-  MICSA_CK(cudaEventRecord(ev[k++], ctx->stream));
+  MICSA_CK(cudaEventRecord(ev[0], ctx->stream));
   for (int64_t it = 0; it < n; it++) {
     for (int ic = 0; ic < g.nc; ic++)
-      for (int p = 0; p < 2; p++) {
+      for (int p = 0; p < 2; p++)
         MICSA_CK(micsa_launch_sweep_micsa(g, p, ic, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
                                           ctx->walk, ctx->stream));
-        MICSA_CK(cudaEventRecord(ev[k++], ctx->stream));
-      }
+    MICSA_CK(cudaEventRecord(ev[2 * it + 1], ctx->stream));
     MICSA_CK(micsa_launch_walk_advance(g, ctx->walk, ctx->stream));
-    MICSA_CK(cudaEventRecord(ev[k++], ctx->stream));
+    MICSA_CK(cudaEventRecord(ev[2 * it + 2], ctx->stream));
   }
   ctx->launches += n * (per + 1);
   MICSA_CK(cudaStreamSynchronize(ctx->stream));
   double sweep = 0, total = 0;
-  k = 0;
   for (int64_t it = 0; it < n; it++) {
-    for (int j = 0; j <= per; j++, k++) {
-      float ms = 0;
-      MICSA_CK(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
-      if (j < per) sweep += ms;
-      total += ms;
-    }
+    float a = 0, b = 0;
+    MICSA_CK(cudaEventElapsedTime(&a, ev[2 * it], ev[2 * it + 1]));
+    MICSA_CK(cudaEventElapsedTime(&b, ev[2 * it + 1], ev[2 * it + 2]));
+    sweep += a;
+    total += a + b;
   }
   for (auto &e : ev) cudaEventDestroy(e);
   if (sweep_ms) *sweep_ms = sweep / (double)(n * per);

@@ -1,0 +1,56 @@
+"""Multi-process plumbing of bench.py on CPU (gloo, world size 2): the
+barrier, the max over ranks that the timed value uses, and the reference
+arm's rank-0-only JSON line.  The path shards as independent replicas (one
+lattice per GPU, no exchange), so these are the only collectives."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _torchrun(args, timeout=300):
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr=127.0.0.1", "--master-port=%d" % _port()] + args
+    env = dict(os.environ, OMP_NUM_THREADS="1", CUDA_VISIBLE_DEVICES="")
+    return subprocess.run(cmd, cwd=ROOT, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                          text=True, timeout=timeout, env=env)
+
+
+def test_dist_barrier_and_max_over_two_gloo_ranks(tmp_path):
+    w = tmp_path / "worker.py"
+    w.write_text(
+        "import sys\n"
+        "sys.path.insert(0, %r)\n"
+        "import bench\n"
+        "d = bench.Dist(backend='gloo')\n"
+        "d.barrier()\n"
+        "v = d.max(1.5 * (d.rank + 1))\n"
+        "d.barrier()\n"
+        "print('RANK %%d WORLD %%d MAX %%.3f' %% (d.rank, d.world, v), flush=True)\n"
+        "d.close()\n" % ROOT)
+    p = _torchrun([str(w)])
+    assert p.returncode == 0, p.stdout[-3000:]
+    for r in (0, 1):
+        assert "RANK %d WORLD 2 MAX 3.000" % r in p.stdout, p.stdout[-3000:]
+
+
+def test_reference_arm_prints_one_line_from_rank_zero():
+    p = _torchrun(["bench.py", "--impl", "reference", "--gpus", "2", "--L", "8", "--nr", "32",
+                   "--nsamples", "1", "--nc", "2", "--steps", "2", "--warmup", "1"])
+    assert p.returncode == 0, p.stdout[-3000:]
+    lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, p.stdout[-3000:]
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
