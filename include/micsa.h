@@ -38,7 +38,7 @@ extern "C" {
 #define MICSA_ERR_STATE 4       /* call not valid in the context's current state */
 #define MICSA_ERR_UNSUPPORTED 5 /* configuration outside what this build supports */
 
-#define MICSA_MAX_SAMPLES 64    /* samples per context (reference: MAXNSAMPLES) */
+#define MICSA_MAX_SAMPLES 4096  /* samples per context (reference: MAXNSAMPLES = 2) */
 
 typedef struct micsa_ctx micsa_ctx;
 
@@ -46,7 +46,7 @@ typedef struct {
   int device;   /* CUDA device ordinal (argv[7], main.cu:39,52-59) */
   int L;        /* lattice side: multiple of 8, 8..1024 (header.h:38-40) */
   int nr;       /* replicas per sample, multiple of 32 (header.h:17 NR) */
-  int nsamples; /* samples simulated together, 1..64 (nbits, main.cu:64) */
+  int nsamples; /* samples simulated together, 1..4096 (nbits, main.cu:64) */
   int nc;       /* demons per site, 1..6 (input.in line 6; d_Walk limit main.cu:1082) */
 } micsa_config;
 
@@ -123,10 +123,11 @@ int micsa_download_spins(micsa_ctx *ctx, int sample, uint64_t *even,
 int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0,
                           uint64_t *w1);
 
-/* Run n microcanonical iterations with CUDA events around every launch and
- * report the mean device time of one half-sweep launch and of one whole
- * iteration, in milliseconds (the per-kernel view of measure_time,
- * timing.c:3-33).  Advances the state like micsa_iterate. */
+/* Run n microcanonical iterations with CUDA events around each iteration's
+ * back-to-back half-sweeps and around its walk, and report the mean device
+ * time of one half-sweep launch and of one whole iteration, in milliseconds
+ * (the per-kernel view of measure_time, timing.c:3-33).  Advances the state
+ * like micsa_iterate. */
 int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration_ms);
 
 /* Text line describing the launch shape the context's autotuner chose at
@@ -160,6 +161,38 @@ int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n);
 int micsa_energy_noalloc(int L, int nr, int nsamples, const uint64_t *even, const uint64_t *odd,
                          const uint64_t *J, int32_t *e_spin, void *stream, char *err,
                          size_t errlen);
+
+/* ---- Batched runs: no counterpart in the reference ----
+ * A job is one reference run of one sample (nbits = 1, nterm = 0, flag 1):
+ * Init (ini.c:8-32) from the job's own seeds -- spins and demon-stream seeds
+ * from seed_u (Init_Random ini.c:34-60, Init_u ini.c:275-299), couplings from
+ * the Janus generator seeded with seed_J (Init_J ini.c:457-471; the
+ * reference's -DJANUS build fixes that seed, a batch gives each job its
+ * own) -- then the main loop (main.cu:130-180): demon refresh at t = 0 and at
+ * every power of two, energies measured at every power of two and at the
+ * end. */
+typedef struct {
+  int L, nr, nc;       /* as in micsa_config */
+  int64_t iterations;  /* maxtime */
+  uint64_t seed_J;     /* coupling seed */
+  uint64_t seed_u;     /* spin / demon-stream seed (0: drawn from /dev/urandom) */
+  double beta;         /* demon temperature (beta.in) */
+} micsa_job;
+/* Measurement points of a job: t = 1, 2, 4, ... <= iterations, plus
+ * iterations itself when it is not a power of two. */
+int64_t micsa_job_measurements(int64_t iterations);
+/* Run njobs jobs of one shape (same L, nr, nc, iterations, beta) together,
+ * job j in sample slot j of one context on `device`: one launch per
+ * half-sweep, refresh and measurement serves every job.  Outputs (either may
+ * be NULL), m the measurement point, nm = micsa_job_measurements:
+ *   e_spin [(j*nm + m)*nr + r]   as micsa_measure's e_spin
+ *   e_demon[(j*nm + m)*nr + r]   as micsa_measure's e_demon
+ * seconds (optional) receives the wall time from context creation to the
+ * last measurement; host initialisation of the jobs (threads, one job per
+ * thread at a time) precedes it.  Each job's numbers equal those of the same
+ * job run alone.  err (optional) receives a message on failure. */
+int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spin,
+                    uint64_t *e_demon, double *seconds, char *err, size_t errlen);
 
 /* Wait for all work issued on the context (cudaDeviceSynchronize,
  * main.cu:144,149) and report any asynchronous error. */

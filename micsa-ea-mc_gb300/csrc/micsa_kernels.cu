@@ -743,7 +743,7 @@ cudaError_t micsa_launch_gen_rnd(const micsa_geo &g, int p, const uint32_t *te,
 }
 
 cudaError_t micsa_launch_walk_advance(const micsa_geo &g, int *walk, cudaStream_t st) {
-  k_walk_advance<<<1, 64, 0, st>>>(walk, g.ns, g.L / 2);
+  k_walk_advance<<<(g.ns + 127) / 128, 128, 0, st>>>(walk, g.ns, g.L / 2);
   return cudaGetLastError();
 }
 

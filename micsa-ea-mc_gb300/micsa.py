@@ -22,7 +22,8 @@ ABI_SYMBOLS = [
     "micsa_set_lut", "micsa_upload_couplings", "micsa_upload_spins", "micsa_upload_demons",
     "micsa_refresh_demons", "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
     "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_energy_noalloc",
-    "micsa_synchronize", "micsa_kernel_launches", "micsa_stream",
+    "micsa_synchronize", "micsa_kernel_launches", "micsa_stream", "micsa_job_measurements",
+    "micsa_run_batch",
 ]
 NOALLOC_MAX_REPLICAS = 8192
 
@@ -48,6 +49,12 @@ class PRC(C.Structure):
 class Xoshiro(C.Structure):
     """micsa_xoshiro_t: the reference's s_xoshiro256pp (48 bytes)."""
     _fields_ = [("s", C.c_uint64 * 4), ("t", C.c_uint64), ("out", C.c_uint64)]
+
+
+class Job(C.Structure):
+    """micsa_job (include/micsa.h): one reference run of one sample."""
+    _fields_ = [("L", C.c_int), ("nr", C.c_int), ("nc", C.c_int), ("iterations", C.c_int64),
+                ("seed_J", C.c_uint64), ("seed_u", C.c_uint64), ("beta", C.c_double)]
 
 
 class RefreshPlan(C.Structure):
@@ -105,6 +112,9 @@ def lib():
         "micsa_synchronize": (C.c_int, [C.c_void_p]),
         "micsa_kernel_launches": (C.c_int64, [C.c_void_p]),
         "micsa_stream": (C.c_void_p, [C.c_void_p]),
+        "micsa_job_measurements": (C.c_int64, [C.c_int64]),
+        "micsa_run_batch": (C.c_int, [C.c_int, C.POINTER(Job), C.c_int, i32p, u64p,
+                                      C.POINTER(C.c_double), C.c_char_p, C.c_size_t]),
         # host side (micsa-ea-mc_gb300/host/micsa_host.h)
         "micsa_check_seed": (C.c_uint64, [C.c_uint64]),
         "micsa_init_cpu_generators": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), u32p, C.c_uint64]),
@@ -418,3 +428,22 @@ class HostModel:
         te = np.zeros(4 * self.nr, np.uint32)
         lib().micsa_fill_bits(self.prc, self.xo, self.nr, it, parity, jobid, _ptr(te, C.c_uint32))
         return te
+
+
+def run_batch(jobs, device=0):
+    """micsa_run_batch over a list of dicts (L, nr, nc, iterations, seed_J,
+    seed_u, beta); returns (e_spin [job, m, nr], e_demon [job, m, nr], seconds)."""
+    n = len(jobs)
+    arr = (Job * n)(*[Job(j["L"], j["nr"], j["nc"], j["iterations"], j["seed_J"], j["seed_u"],
+                          j["beta"]) for j in jobs])
+    nm = lib().micsa_job_measurements(jobs[0]["iterations"])
+    nr = jobs[0]["nr"]
+    es = np.zeros(n * nm * nr, np.int32)
+    ed = np.zeros(n * nm * nr, np.uint64)
+    sec = C.c_double()
+    err = C.create_string_buffer(512)
+    rc = lib().micsa_run_batch(device, arr, n, _ptr(es, C.c_int32), _ptr(ed, C.c_uint64),
+                               C.byref(sec), err, 512)
+    if rc != MICSA_OK:
+        raise MicsaError("micsa_run_batch: %s %s" % (STATUS.get(rc, rc), err.value.decode()))
+    return es.reshape(n, nm, nr), ed.reshape(n, nm, nr), sec.value

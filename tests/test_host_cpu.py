@@ -36,7 +36,7 @@ def test_create_without_gpu_fails_cleanly():
 
 def test_invalid_configs_rejected_before_cuda():
     for bad in [(0, 12, 32, 1, 6), (0, 16, 48, 1, 6), (0, 16, 32, 0, 6), (0, 16, 32, 1, 0),
-                (0, 16, 32, 65, 6), (0, 16, 32, 1, 7)]:
+                (0, 16, 32, 4097, 6), (0, 16, 32, 1, 7)]:
         cfg = micsa.Config(*bad)
         assert micsa.lib().micsa_footprint_bytes(C.byref(cfg)) == -1
         h = C.c_void_p()
