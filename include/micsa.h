@@ -102,7 +102,11 @@ int micsa_refresh_demons(micsa_ctx *ctx, int first, int count, void *prc, void *
 int micsa_monte_carlo(micsa_ctx *ctx, int flag, const uint32_t *te,
                       const uint32_t *keys);
 /* n microcanonical iterations back to back (flag = 1 each), replayed from a
- * CUDA graph of one iteration.  Asynchronous. */
+ * CUDA graph of one iteration; at L = 8 and 16 (where a sample's state fits
+ * in one block's shared memory) up to 1024 whole iterations per launch of a
+ * shared-memory-resident kernel instead (MICSA_RESIDENT=0 in the environment
+ * at micsa_create turns that off).  Results are identical either way.
+ * Asynchronous. */
 int micsa_iterate(micsa_ctx *ctx, int64_t n);
 
 /* Measurements of every sample at the current state (Measure_Energy_Spins

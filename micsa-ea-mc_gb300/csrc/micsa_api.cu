@@ -37,6 +37,7 @@ struct micsa_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int64_t launches = 0;
+  int resident = 0;        /* small lattice: iterations run in shared memory */
   int ntune = 0;           /* launch shapes timed at creation */
   int tune_zc[MICSA_TUNE_MAX] = {0}, tune_pd[MICSA_TUNE_MAX] = {0};
   double tune_ms[MICSA_TUNE_MAX] = {0};
@@ -293,6 +294,15 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem0, 0, 4 * s.dem_w, ctx->stream));
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem1, 0, 4 * s.dem_w, ctx->stream));
   MICSA_CK_CREATE(cudaStreamSynchronize(ctx->stream));
+  {
+    /* MICSA_RESIDENT=0 keeps small lattices on the per-half-sweep kernels */
+    const char *er = getenv("MICSA_RESIDENT");
+    const size_t need = micsa_resident_smem(cfg->L, cfg->nc);
+    int optin = 0;
+    MICSA_CK_CREATE(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                           cfg->device));
+    ctx->resident = need > 0 && need <= (size_t)optin && !(er && !strcmp(er, "0"));
+  }
   if ((rc = autotune(ctx)) != MICSA_OK) {
     fprintf(stderr, "micsa_create: autotune: %s\n", ctx->err);
     micsa_destroy(ctx);
@@ -560,7 +570,7 @@ int micsa_iterate(micsa_ctx *ctx, int64_t n) {
   if (!ctx || n < 0) return fail(ctx, MICSA_ERR_ARG, "bad argument");
   int rc = set_device(ctx);
   if (rc || (rc = ready_for_sweeps(ctx, 1))) return rc;
-  if (!ctx->graph_exec) {
+  if (!ctx->graph_exec && !ctx->resident) {
     MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     rc = enqueue_micsa_iteration(ctx);
     cudaGraph_t graph = nullptr;
@@ -572,6 +582,17 @@ int micsa_iterate(micsa_ctx *ctx, int64_t n) {
     MICSA_CK(e);
     ctx->graph = graph;
     MICSA_CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
+  }
+  if (ctx->resident) {
+    /* small lattices: whole iterations in shared memory, up to 1024 per launch */
+    for (int64_t done = 0; done < n;) {
+      const int m = (int)(n - done < 1024 ? n - done : 1024);
+      MICSA_CK(micsa_launch_resident(ctx->g, m, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
+                                     ctx->walk, ctx->stream));
+      ctx->launches += 2;
+      done += m;
+    }
+    return MICSA_OK;
   }
   for (int64_t i = 0; i < n; i++) MICSA_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
   ctx->launches += n * (2 * ctx->g.nc + 1);

@@ -914,3 +914,123 @@ cudaError_t micsa_launch_refresh(const micsa_geo &g, int first, int count, int64
                                                         dem0, dem1);
   return cudaGetLastError();
 }
+
+/* --------------------------------------------- resident small lattices */
+/* At L <= 16 one sample's spins, coupling bytes and demon planes of one
+ * 32-replica word -- 2P*4 + 2P + 2*(2*nc*P*4) bytes, 216 KB at L=16, nc=6 --
+ * fit in one block's shared memory.  Block (w, s) copies them in, runs n
+ * iterations (2*nc half-sweeps with a barrier after each, the demon walk as
+ * the translation k -> k+1 mod L/2, as in the other kernels) and copies them
+ * back; HBM is touched only at the ends.  The per-site arithmetic is
+ * k_sweep's; shared memory has no coalescing constraint, so a thread takes
+ * one site at a time.  The walk counter is only read here: the caller
+ * advances it by n afterwards. */
+template <int L>
+struct resident_cfg {
+  static constexpr int P = L * L * L / 2, Lh = L / 2;
+  static constexpr int TPB = P < 512 ? P : 512;
+};
+
+template <int L>
+__global__ void __launch_bounds__(resident_cfg<L>::TPB)
+k_resident(const micsa_geo g, const int n, uint32_t *__restrict__ spin,
+           uint32_t *__restrict__ d0, uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
+           const int *__restrict__ walk) {
+  constexpr int P = resident_cfg<L>::P, Lh = resident_cfg<L>::Lh, TPB = resident_cfg<L>::TPB;
+  extern __shared__ uint4 smem_raw[];
+  const int w = blockIdx.x, s = blockIdx.y, W = g.W, nc = g.nc;
+  uint32_t *sp = (uint32_t *)smem_raw; /* [2][P] */
+  uint32_t *sd0 = sp + 2 * P;          /* [2][nc][P] */
+  uint32_t *sd1 = sd0 + 2 * nc * P;
+  uint8_t *sj = (uint8_t *)(sd1 + 2 * nc * P); /* [2][P] */
+  const size_t sbase = (size_t)s * 2 * P, dbase = (size_t)s * 2 * nc * P;
+  for (int i = threadIdx.x; i < 2 * P; i += TPB) {
+    sp[i] = spin[(sbase + i) * W + w];
+    sj[i] = jb[sbase + i];
+  }
+  for (int i = threadIdx.x; i < 2 * nc * P; i += TPB) {
+    sd0[i] = d0[(dbase + i) * W + w];
+    sd1[i] = d1[(dbase + i) * W + w];
+  }
+  int k = walk[s];
+  __syncthreads();
+  for (int it = 0; it < n; it++) {
+    for (int ic = 0; ic < nc; ic++) {
+      const int axis = ic < 3 ? ic : ic - 3;
+      for (int p = 0; p < 2; p++) {
+        const int sh = ((p == 0) == (ic < 3)) ? k : -k; /* demon shift, units of 2 sites */
+        const uint32_t *oth = sp + (p ^ 1) * P;
+        uint32_t *mine = sp + p * P;
+        uint32_t *q0 = sd0 + (p * nc + ic) * P, *q1 = sd1 + (p * nc + ic) * P;
+        const uint8_t *jp = sj + p * P;
+#pragma unroll
+        for (int i = threadIdx.x; i < P; i += TPB) {
+          const int xh = i % Lh, y = (i / Lh) % L, z = i / (Lh * L);
+          const int rowoff = (y + z + p) & 1;
+          int xe = xh + rowoff; if (xe == Lh) xe = 0;
+          int xo = xh + rowoff - 1; if (xo < 0) xo = Lh - 1;
+          const int yp = (y + 1) & (L - 1), ym = (y - 1) & (L - 1);
+          const int zp = (z + 1) & (L - 1), zm = (z - 1) & (L - 1);
+          const int row = (z * L + y) * Lh;
+          const uint32_t sw = mine[i];
+          const uint32_t jb6 = jp[i];
+          const uint32_t f0 = sw ^ oth[row + xe] ^ jmask(jb6, 0);
+          const uint32_t f1 = sw ^ oth[(z * L + yp) * Lh + xh] ^ jmask(jb6, 1);
+          const uint32_t f2 = sw ^ oth[(zp * L + y) * Lh + xh] ^ jmask(jb6, 2);
+          const uint32_t f3 = sw ^ oth[row + xo] ^ jmask(jb6, 3);
+          const uint32_t f4 = sw ^ oth[(z * L + ym) * Lh + xh] ^ jmask(jb6, 4);
+          const uint32_t f5 = sw ^ oth[(zm * L + y) * Lh + xh] ^ jmask(jb6, 5);
+          const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
+          const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+          int slot;
+          if (axis == 0) slot = row + ((xh - sh) & (Lh - 1));
+          else if (axis == 1) slot = (z * L + ((y - 2 * sh) & (L - 1))) * Lh + xh;
+          else slot = (((z - 2 * sh) & (L - 1)) * L + y) * Lh + xh;
+          uint32_t D0 = q0[slot], D1 = q1[slot];
+          const uint32_t flip = isi_update(j1, j2, j3, j4, D0, D1);
+          q0[slot] = D0;
+          q1[slot] = D1;
+          mine[i] = sw ^ flip;
+        }
+        __syncthreads();
+      }
+    }
+    k = (k + 1 == Lh) ? 0 : k + 1;
+  }
+  for (int i = threadIdx.x; i < 2 * P; i += TPB) spin[(sbase + i) * W + w] = sp[i];
+  for (int i = threadIdx.x; i < 2 * nc * P; i += TPB) {
+    d0[(dbase + i) * W + w] = sd0[i];
+    d1[(dbase + i) * W + w] = sd1[i];
+  }
+}
+
+__global__ void k_walk_add(int *walk, int ns, int n, int period) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < ns) walk[s] = (int)(((int64_t)walk[s] + n) % period);
+}
+
+size_t micsa_resident_smem(int L, int nc) {
+  if (L != 8 && L != 16) return 0;
+  const size_t P = (size_t)L * L * L / 2;
+  return 2 * P * 4 + 2 * P + 2 * (2 * (size_t)nc * P * 4);
+}
+
+template <int L>
+static cudaError_t resident_l(const micsa_geo &g, int n, uint32_t *spin, uint32_t *d0,
+                              uint32_t *d1, const uint8_t *jb, int *walk, cudaStream_t st) {
+  const size_t bytes = micsa_resident_smem(L, g.nc);
+  cudaError_t e = cudaFuncSetAttribute(k_resident<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bytes);
+  if (e != cudaSuccess) return e;
+  k_resident<L><<<dim3(g.W, g.ns), resident_cfg<L>::TPB, bytes, st>>>(g, n, spin, d0, d1, jb, walk);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  k_walk_add<<<(g.ns + 127) / 128, 128, 0, st>>>(walk, g.ns, n, g.L / 2);
+  return cudaGetLastError();
+}
+
+cudaError_t micsa_launch_resident(const micsa_geo &g, int n, uint32_t *spin, uint32_t *d0,
+                                  uint32_t *d1, const uint8_t *jb, int *walk, cudaStream_t st) {
+  if (g.L == 8) return resident_l<8>(g, n, spin, d0, d1, jb, walk, st);
+  if (g.L == 16) return resident_l<16>(g, n, spin, d0, d1, jb, walk, st);
+  return cudaErrorInvalidValue;
+}

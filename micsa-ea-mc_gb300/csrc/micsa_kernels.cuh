@@ -85,4 +85,11 @@ cudaError_t micsa_launch_refresh(const micsa_geo &g, int first, int count, int64
                                  const uint64_t *fib, const uint64_t thr[3],
                                  uint32_t *dem0, uint32_t *dem1, cudaStream_t st);
 
+/* Shared-memory bytes of the resident small-lattice kernel for this L and
+ * nc (0: L not supported by it), and its launch: n whole iterations of all
+ * samples, walk counters advanced by n. */
+size_t micsa_resident_smem(int L, int nc);
+cudaError_t micsa_launch_resident(const micsa_geo &g, int n, uint32_t *spin, uint32_t *d0,
+                                  uint32_t *d1, const uint8_t *jb, int *walk, cudaStream_t st);
+
 #endif
