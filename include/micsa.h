@@ -91,6 +91,15 @@ int micsa_upload_demons(micsa_ctx *ctx, int sample, const uint64_t *w0,
  * draws on host threads. */
 int micsa_refresh_demons(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
                          const uint64_t *thr);
+/* The same refresh, returning as soon as the device work is queued: the
+ * advance of the caller's structs runs on host threads meanwhile, while the
+ * GPU draws and runs whatever is queued after it.  Until micsa_refresh_wait
+ * returns (or the next refresh call on this context, or micsa_destroy) the
+ * caller must neither read, write nor free prc and xo.  No counterpart in
+ * the reference. */
+int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
+                               const uint64_t *thr);
+int micsa_refresh_wait(micsa_ctx *ctx);
 
 /* One iteration of Monte_Carlo (main.cu:197-313) on all samples.
  *   flag = 1: nc x (even, odd) microcanonical half-sweeps, then the demon

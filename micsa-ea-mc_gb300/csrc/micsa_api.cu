@@ -11,6 +11,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <new>
 #include <thread>
 #include <vector>
@@ -44,8 +45,10 @@ struct micsa_ctx {
   /* demon refresh on the device: jump tables of one segment length */
   micsa_refresh_plan plan = {};
   uint64_t *plan_lcg = nullptr, *plan_xo = nullptr, *plan_fib = nullptr;
-  uint64_t *rec = nullptr;
+  uint64_t *rec = nullptr, *rec_host = nullptr; /* start records: device, pinned staging */
   size_t rec_words = 0;
+  cudaEvent_t rec_copied = nullptr;  /* staging upload done */
+  std::thread advancer;              /* host advance of the last refresh's streams */
   char err[512] = {0};
 };
 
@@ -145,6 +148,26 @@ int ready_for_sweeps(micsa_ctx *ctx, int need_demons) {
       return fail(ctx, MICSA_ERR_STATE, "sample %d has no demons uploaded", s);
   }
   return MICSA_OK;
+}
+
+/* f(s0, s1) over [0, n) on up to hardware_concurrency threads, at least
+ * `grain` items each; the calling thread takes the first share */
+template <class F>
+void parallel_for(int64_t n, int64_t grain, F f) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  int64_t nt = n / (grain > 0 ? grain : 1);
+  if (nt > (int64_t)(hw ? hw : 1)) nt = hw ? hw : 1;
+  if (nt < 1) nt = 1;
+  std::vector<std::thread> pool;
+  for (int64_t t = 1; t < nt; t++) {
+    try {
+      pool.emplace_back(f, n * t / nt, n * (t + 1) / nt);
+    } catch (...) {
+      f(n * t / nt, n * (t + 1) / nt);
+    }
+  }
+  f(0, n / nt);
+  for (auto &th : pool) th.join();
 }
 
 /* Slab-depth autotuner: time a (colour 0, colour 1) pair of micSA
@@ -328,6 +351,7 @@ int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
 
 int micsa_destroy(micsa_ctx *ctx) {
   if (!ctx) return MICSA_OK;
+  if (ctx->advancer.joinable()) ctx->advancer.join();
   cudaSetDevice(ctx->cfg.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
@@ -339,6 +363,8 @@ int micsa_destroy(micsa_ctx *ctx) {
     if (b) cudaFree(b);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   micsa_refresh_plan_free(&ctx->plan);
+  if (ctx->rec_host) cudaFreeHost(ctx->rec_host);
+  if (ctx->rec_copied) cudaEventDestroy(ctx->rec_copied);
   delete ctx;
   return MICSA_OK;
 }
@@ -474,70 +500,95 @@ int ensure_refresh_plan(micsa_ctx *ctx, int64_t nw, int wps) {
 
 }  // namespace
 
-int micsa_refresh_demons(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
-                         const uint64_t *thr) {
+int micsa_refresh_wait(micsa_ctx *ctx) {
+  if (!ctx) return MICSA_ERR_ARG;
+  if (ctx->advancer.joinable()) ctx->advancer.join();
+  return MICSA_OK;
+}
+
+int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
+                               const uint64_t *thr) {
   if (!ctx || !prc || !xo || !thr) return fail(ctx, MICSA_ERR_ARG, "null argument");
   if (first < 0 || count < 1 || first + count > ctx->cfg.nsamples)
     return fail(ctx, MICSA_ERR_ARG, "samples [%d, %d) out of range [0, %d)", first, first + count,
                 ctx->cfg.nsamples);
+  micsa_refresh_wait(ctx); /* the previous refresh's structs may be these */
   int rc = set_device(ctx);
   if (rc) return rc;
   const micsa_geo &g = ctx->g;
   micsa_prc_t *P = (micsa_prc_t *)prc;
   micsa_xoshiro_t *X = (micsa_xoshiro_t *)xo;
   const int64_t nw = 2 * g.H * g.nc, nstreams = (int64_t)count * g.nr;
+  const size_t words = (size_t)nstreams * MICSA_STREAM_REC;
   /* segments of 32 words (2048 draws), shorter when the call has few warps */
   int wps = 32;
   while (wps > 2 && (int64_t)count * g.W * ((nw + wps - 1) / wps) < 4096) wps >>= 1;
 
-  /* start records, grouped by warp; checked before anything changes */
-  std::vector<uint64_t> rec((size_t)nstreams * MICSA_STREAM_REC);
-  uint64_t one[MICSA_STREAM_REC];
-  for (int64_t s = 0; s < nstreams; s++) {
-    if (micsa_stream_record(&P[s], &X[s], one))
-      return fail(ctx, MICSA_ERR_ARG, "stream %lld: PR ring pointers are not 24, 55, 61 apart",
-                  (long long)s);
-    const int64_t grp = s / 32, lane = s % 32;
-    for (int k = 0; k < MICSA_STREAM_REC; k++) rec[(grp * MICSA_STREAM_REC + k) * 32 + lane] = one[k];
-  }
-  if ((rc = ensure_refresh_plan(ctx, nw, wps))) return rc;
-  if (ctx->rec_words < rec.size()) {
+  /* pinned staging for the start records; the previous upload from it must
+   * have completed before it is rewritten */
+  if (ctx->rec_copied) MICSA_CK(cudaEventSynchronize(ctx->rec_copied));
+  if (ctx->rec_words < words) {
     MICSA_CK(cudaStreamSynchronize(ctx->stream));
     if (ctx->rec) cudaFree(ctx->rec);
-    ctx->rec = nullptr;
-    MICSA_CK(cudaMalloc(&ctx->rec, rec.size() * sizeof(uint64_t)));
-    ctx->rec_words = rec.size();
+    if (ctx->rec_host) cudaFreeHost(ctx->rec_host);
+    ctx->rec = ctx->rec_host = nullptr;
+    ctx->rec_words = 0;
+    MICSA_CK(cudaMalloc(&ctx->rec, words * sizeof(uint64_t)));
+    MICSA_CK(cudaHostAlloc(&ctx->rec_host, words * sizeof(uint64_t), cudaHostAllocDefault));
+    ctx->rec_words = words;
   }
-  /* pageable source: the call returns once the words are staged */
-  MICSA_CK(cudaMemcpyAsync(ctx->rec, rec.data(), rec.size() * sizeof(uint64_t),
-                           cudaMemcpyHostToDevice, ctx->stream));
+  if (!ctx->rec_copied) MICSA_CK(cudaEventCreateWithFlags(&ctx->rec_copied, cudaEventDisableTiming));
+
+  /* start records, grouped by warp, built in parallel; checked before
+   * anything on the device changes */
+  uint64_t *rec = ctx->rec_host;
+  std::atomic<int64_t> bad(-1);
+  parallel_for(nstreams, 256, [&](int64_t s0, int64_t s1) {
+    uint64_t one[MICSA_STREAM_REC];
+    for (int64_t s = s0; s < s1; s++) {
+      if (micsa_stream_record(&P[s], &X[s], one)) {
+        bad.store(s);
+        continue;
+      }
+      const int64_t grp = s / 32, lane = s % 32;
+      for (int k = 0; k < MICSA_STREAM_REC; k++) rec[(grp * MICSA_STREAM_REC + k) * 32 + lane] = one[k];
+    }
+  });
+  if (bad.load() >= 0)
+    return fail(ctx, MICSA_ERR_ARG, "stream %lld: PR ring pointers are not 24, 55, 61 apart",
+                (long long)bad.load());
+  if ((rc = ensure_refresh_plan(ctx, nw, wps))) return rc;
+  MICSA_CK(cudaMemcpyAsync(ctx->rec, rec, words * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  MICSA_CK(cudaEventRecord(ctx->rec_copied, ctx->stream));
   MICSA_CK(micsa_launch_refresh(g, first, count, nw, wps, ctx->plan.nseg, ctx->rec, ctx->plan_lcg,
                                 ctx->plan_xo, ctx->plan_fib, thr, ctx->dem0, ctx->dem1,
                                 ctx->stream));
   ctx->launches++;
   MICSA_CK(cudaMemsetAsync(ctx->walk + first, 0, count * sizeof(int), ctx->stream));
-
-  /* the caller's streams move past the draws while the device makes them */
-  const micsa_refresh_plan *plan = &ctx->plan;
-  auto advance = [=](int64_t s0, int64_t s1) {
-    for (int64_t s = s0; s < s1; s++) micsa_streams_advance_plan(plan, &P[s], &X[s]);
-  };
-  unsigned hw = std::thread::hardware_concurrency();
-  int64_t nt = nstreams / 64;
-  if (nt > (int64_t)hw) nt = hw;
-  if (nt < 1) nt = 1;
-  std::vector<std::thread> pool;
-  for (int64_t t = 1; t < nt; t++) {
-    try {
-      pool.emplace_back(advance, nstreams * t / nt, nstreams * (t + 1) / nt);
-    } catch (...) {
-      advance(nstreams * t / nt, nstreams * (t + 1) / nt);
-    }
-  }
-  advance(0, nstreams / nt);
-  for (auto &th : pool) th.join();
   for (int s = first; s < first + count; s++) ctx->have_dem[s] = 1;
+
+  /* the caller's streams move past the draws on host threads while the
+   * device draws (and runs whatever is queued next) */
+  const micsa_refresh_plan *plan = &ctx->plan;
+  auto advance = [plan, P, X, nstreams]() {
+    parallel_for(nstreams, 64, [&](int64_t s0, int64_t s1) {
+      for (int64_t s = s0; s < s1; s++) micsa_streams_advance_plan(plan, &P[s], &X[s]);
+    });
+  };
+  try {
+    ctx->advancer = std::thread(advance);
+  } catch (...) {
+    advance();
+  }
   return MICSA_OK;
+}
+
+int micsa_refresh_demons(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
+                         const uint64_t *thr) {
+  const int rc = micsa_refresh_demons_async(ctx, first, count, prc, xo, thr);
+  micsa_refresh_wait(ctx);
+  return rc;
 }
 
 int micsa_monte_carlo(micsa_ctx *ctx, int flag, const uint32_t *te, const uint32_t *keys) {

@@ -175,7 +175,8 @@ int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spi
     }
     int64_t t = 0, m = 0;
     while (t < j0->iterations) {
-      if (!(t & (t - 1))) CK(micsa_refresh_demons(ctx, 0, njobs, prc, xo, thr));
+      /* the host advance of the streams overlaps the iterations that follow */
+      if (!(t & (t - 1))) CK(micsa_refresh_demons_async(ctx, 0, njobs, prc, xo, thr));
       int64_t next = 1;
       while (next <= t) next <<= 1;
       if (next > j0->iterations) next = j0->iterations;

@@ -20,7 +20,8 @@ STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE", 
 ABI_SYMBOLS = [
     "micsa_create", "micsa_destroy", "micsa_last_error", "micsa_footprint_bytes",
     "micsa_set_lut", "micsa_upload_couplings", "micsa_upload_spins", "micsa_upload_demons",
-    "micsa_refresh_demons", "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
+    "micsa_refresh_demons", "micsa_refresh_demons_async", "micsa_refresh_wait",
+    "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
     "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_energy_noalloc",
     "micsa_synchronize", "micsa_kernel_launches", "micsa_stream", "micsa_job_measurements",
     "micsa_run_batch",
@@ -98,6 +99,9 @@ def lib():
         "micsa_upload_demons": (C.c_int, [C.c_void_p, C.c_int, u64p, u64p]),
         "micsa_refresh_demons": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(PRC),
                                            C.POINTER(Xoshiro), u64p]),
+        "micsa_refresh_demons_async": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(PRC),
+                                                 C.POINTER(Xoshiro), u64p]),
+        "micsa_refresh_wait": (C.c_int, [C.c_void_p]),
         "micsa_monte_carlo": (C.c_int, [C.c_void_p, C.c_int, u32p, u32p]),
         "micsa_iterate": (C.c_int, [C.c_void_p, C.c_int64]),
         "micsa_measure": (C.c_int, [C.c_void_p, i32p, u64p, i64p, i64p]),
@@ -222,6 +226,20 @@ class Context:
         t = np.ascontiguousarray(thr, dtype=np.uint64)
         check(self.h, lib().micsa_refresh_demons(self.h, first, count, prc, xo, _ptr(t, C.c_uint64)),
               "refresh_demons")
+
+    def refresh_demons_async(self, first, prc, xo, thr):
+        """As refresh_demons; prc/xo are advanced in the background until
+        refresh_wait (keep them alive and untouched until then)."""
+        count, rem = divmod(len(prc), self.nr)
+        if rem or len(xo) != len(prc):
+            raise ValueError("need count*nr streams of each generator")
+        self._thr = np.ascontiguousarray(thr, dtype=np.uint64)
+        check(self.h, lib().micsa_refresh_demons_async(self.h, first, count, prc, xo,
+                                                       _ptr(self._thr, C.c_uint64)),
+              "refresh_demons_async")
+
+    def refresh_wait(self):
+        check(self.h, lib().micsa_refresh_wait(self.h), "refresh_wait")
 
     def monte_carlo(self, flag, te=None, keys=None):
         t = None if te is None else np.ascontiguousarray(te, dtype=np.uint32)

@@ -115,3 +115,35 @@ def test_gpu_refresh_full_size_headline_shape():
             g0, g1 = ctx.download_demons(s)
             assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
         assert bytes(prc) == bytes(hp) and bytes(xo) == bytes(hx)
+
+
+def test_gpu_refresh_async_overlaps_and_matches():
+    """micsa_refresh_demons_async: iterations queued right after it run while
+    the host advances the streams; after refresh_wait the structs and the
+    demons equal those of the synchronous call."""
+    L, nr, nc, ns = 16, 64, 6, 2
+    thr = micsa.thresholds(BETA)
+    rng = np.random.default_rng(11)
+    H, V = (L // 4) ** 3 // 2, L ** 3
+    prc, xo = _streams(ns * nr, 321)
+    hp, hx = _copy(prc, micsa.PRC), _copy(xo, micsa.Xoshiro)
+    out = []
+    for asyn, (p_, x_) in ((True, (prc, xo)), (False, (hp, hx))):
+        r2 = np.random.default_rng(5)
+        with micsa.Context(L, nr, ns, nc) as ctx:
+            for s in range(ns):
+                J = micsa.pack_couplings(L, *(r2.integers(0, 2, size=V, dtype=np.uint8) for _ in range(3)))
+                ctx.upload_couplings(s, J)
+                ctx.upload_spins(s, *(r2.integers(0, 2 ** 64 - 1, size=H * nr, dtype=np.uint64,
+                                                  endpoint=True) for _ in range(2)))
+            for rnd in range(3):
+                if asyn:
+                    ctx.refresh_demons_async(0, p_, x_, thr)
+                else:
+                    ctx.refresh_demons(0, p_, x_, thr)
+                ctx.iterate(3)
+            ctx.refresh_wait()
+            out.append([ctx.download_demons(s) for s in range(ns)] + [ctx.download_spins(s) for s in range(ns)])
+    assert bytes(prc) == bytes(hp) and bytes(xo) == bytes(hx)
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
