@@ -44,14 +44,21 @@ def parse():
     # smaller shapes for profiling captures (the headline is the default)
     ap.add_argument("--L", type=int, default=160)
     ap.add_argument("--nr", type=int, default=64)
-    ap.add_argument("--nsamples", type=int, default=2)
+    ap.add_argument("--nsamples", type=int, default=None,
+                    help="samples (plain, default 2) or jobs (batched, default 512)")
     ap.add_argument("--nc", type=int, default=6)
     ap.add_argument("--workload", default="plain", choices=["plain", "batched"],
                     help="plain: the headline run; batched: --nsamples jobs per context")
-    ap.add_argument("--iterations", type=int, default=4096, help="batched: iterations per job")
+    ap.add_argument("--iterations", type=int, default=4096,
+                    help="batched with --batch-L: iterations per job")
+    ap.add_argument("--batch-L", type=int, default=None,
+                    help="batched: one lattice size instead of the mixed-L stream")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.nsamples is None:
+        a.nsamples = 512 if a.workload == "batched" else 2
+    return a
 
 
 class Dist:
@@ -405,29 +412,52 @@ def config(a):
             "parallelism": "replicas (an independent lattice per GPU)"}
 
 
+BATCH_L = (8, 16, 24, 32, 48)          # L = 12 is not a legal size (multiple of 8)
+BATCH_SWEEPS = (1 << 10, 1 << 12, 1 << 14)
+
+
+def batched_jobs(a):
+    """The batched configuration: a.nsamples jobs, L uniform in BATCH_L and
+    sweeps uniform in BATCH_SWEEPS (or one shape with --batch-L), 64
+    replicas, independent seeds from master seed 20260101."""
+    rng = np.random.default_rng(20260101)
+    n = a.nsamples
+    Ls = rng.choice(BATCH_L, size=n) if a.batch_L is None else np.full(n, a.batch_L)
+    its = rng.choice(BATCH_SWEEPS, size=n) if a.batch_L is None else np.full(n, a.iterations)
+    seeds = rng.integers(1, 2 ** 63 - 1, size=(n, 2), dtype=np.int64)
+    return [dict(L=int(L), nr=a.nr, nc=a.nc, iterations=int(it), seed_J=int(sj), seed_u=int(su),
+                 beta=BETA) for L, it, (sj, su) in zip(Ls, its, seeds)]
+
+
 def run_batched(a, dist):
-    """Batched configuration: a.nsamples independent reference runs (jobs) of
-    L, 64 replicas, nc demons, a.iterations iterations each, on the
-    reference's refresh/measurement schedule, through micsa_run_batch (host
-    initialisation of the jobs outside the timed part; context creation,
-    uploads, GPU refreshes, iterations and measurement readbacks inside)."""
+    """All jobs through micsa_run_batch (host initialisation of the jobs
+    outside the timed part; context creation, uploads, GPU refreshes,
+    iterations and measurement readbacks inside), against the plain path of
+    one micsa_run_batch call per job, timed on one job of every (L, sweeps)
+    pair and weighted by the pair counts."""
+    import collections
     import micsa
-    master = np.random.default_rng(20260101)
-    seeds = master.integers(1, 2 ** 63 - 1, size=(a.nsamples, 2), dtype=np.int64)
-    jobs = [dict(L=a.L, nr=a.nr, nc=a.nc, iterations=a.iterations, seed_J=int(sj), seed_u=int(su),
-                 beta=BETA) for sj, su in seeds]
+    jobs = batched_jobs(a)
     for _ in range(max(0, a.warmup)):
-        micsa.run_batch(jobs[:min(8, len(jobs))], device=dist.local)
+        micsa.run_batch(jobs[:4], device=dist.local)
     dist.barrier()
-    t0 = time.perf_counter()
     es, ed, sec = micsa.run_batch(jobs, device=dist.local)
-    wall = dist.max(time.perf_counter() - t0)
     sec = dist.max(sec)
-    attempts = float(a.L ** 3) * a.nr * a.nc * a.iterations * a.nsamples
-    return {"value": round(attempts * dist.world / (sec * 1e12), 4),
-            "ms_per_step": round(sec * 1e3 / a.iterations, 5),
-            "job_seconds": round(sec, 4), "wall_seconds_with_host_init": round(wall, 3),
-            "measurements": int(es.shape[1])}
+    attempts = sum(float(j["L"] ** 3) * j["nr"] * j["nc"] * j["iterations"] for j in jobs)
+    count = collections.Counter((j["L"], j["iterations"]) for j in jobs)
+    plain, per = 0.0, {}
+    for key in sorted(count):
+        job = next(j for j in jobs if (j["L"], j["iterations"]) == key)
+        _, _, t1 = micsa.run_batch([job], device=dist.local)
+        per["L%d_%d" % key] = round(t1, 4)
+        plain += count[key] * t1
+    return {"anneals_per_s": round(len(jobs) * dist.world / sec, 2),
+            "plain_anneals_per_s": round(len(jobs) / plain, 2),
+            "speedup_vs_plain": round(plain / sec, 2),
+            "attempts_per_ps": round(attempts * dist.world / (sec * 1e12), 4),
+            "job_seconds": round(sec, 4), "plain_seconds_estimated": round(plain, 3),
+            "plain_seconds_per_job": per, "jobs": len(jobs),
+            "pairs": {"L%d_%d" % k: v for k, v in sorted(count.items())}}
 
 
 def main():
@@ -441,18 +471,21 @@ def main():
             return
         r = run_batched(a, dist)
         if dist.rank == 0:
+            mixed = a.batch_L is None
             print(json.dumps({
-                "metric": "spin-flips/ps, batched jobs at L=%d" % a.L, "unit": UNIT,
-                "value": r["value"], "n_gpus": dist.world, "steps": a.iterations,
-                "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "metric": "anneals/s, batched %s" % ("mixed-L stream" if mixed else "L=%d" % a.batch_L),
+                "unit": "anneals/s", "value": r["anneals_per_s"], "n_gpus": dist.world,
+                "steps": a.nsamples, "warmup": a.warmup,
+                "ms_per_step": round(r["job_seconds"] * 1e3 / a.nsamples, 4),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
                 "data": "synthetic: %d jobs seeded from master seed 20260101" % a.nsamples,
-                "config": {"workload": "batched: %d independent reference runs (1 sample each) of "
-                                       "L=%d, %d replicas, nc=%d, %d iterations on the reference "
-                                       "schedule, one context" % (a.nsamples, a.L, a.nr, a.nc,
-                                                                  a.iterations),
-                           "L": a.L, "replicas": a.nr, "jobs": a.nsamples, "nc": a.nc,
-                           "iterations": a.iterations},
+                "config": {"workload": "batched: %d independent reference runs (1 sample each), L "
+                                       "uniform in %s, sweeps uniform in %s, %d replicas, nc=%d, "
+                                       "reference refresh/measurement schedule" % (
+                                           a.nsamples, list(BATCH_L) if mixed else [a.batch_L],
+                                           list(BATCH_SWEEPS) if mixed else [a.iterations],
+                                           a.nr, a.nc),
+                           "jobs": a.nsamples, "replicas": a.nr, "nc": a.nc},
                 "detail": r}))
         dist.close()
         return

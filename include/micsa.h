@@ -194,18 +194,31 @@ typedef struct {
 /* Measurement points of a job: t = 1, 2, 4, ... <= iterations, plus
  * iterations itself when it is not a power of two. */
 int64_t micsa_job_measurements(int64_t iterations);
-/* Run njobs jobs of one shape (same L, nr, nc, iterations, beta) together,
- * job j in sample slot j of one context on `device`: one launch per
- * half-sweep, refresh and measurement serves every job.  Outputs (either may
- * be NULL), m the measurement point, nm = micsa_job_measurements:
- *   e_spin [(j*nm + m)*nr + r]   as micsa_measure's e_spin
- *   e_demon[(j*nm + m)*nr + r]   as micsa_measure's e_demon
- * seconds (optional) receives the wall time from context creation to the
- * last measurement; host initialisation of the jobs (threads, one job per
- * thread at a time) precedes it.  Each job's numbers equal those of the same
- * job run alone.  err (optional) receives a message on failure. */
+/* Run njobs jobs together.  Jobs of one shape (L, nr, nc, beta) share a
+ * context, one job per sample slot, longest first; each shape group runs in
+ * its own context and stream on `device`, concurrently with the others.  In
+ * a group one launch per half-sweep (or per 1024 iterations at L <= 16),
+ * refresh and measurement serves every running job; a job whose iterations
+ * are done is frozen (micsa_set_active) after its last measurement.
+ * Outputs (either may be NULL), m = measurement point, nm_j =
+ * micsa_job_measurements(jobs[j].iterations), off_j = sum over i < j of
+ * nm_i * nr_i:
+ *   e_spin [off_j + m*nr_j + r]   as micsa_measure's e_spin
+ *   e_demon[off_j + m*nr_j + r]   as micsa_measure's e_demon
+ * seconds (optional) receives the wall time from the first context's
+ * creation to the end of the last group; host initialisation of the jobs
+ * (on threads) precedes it.  Each job's numbers equal those of the same job
+ * run alone.  err (optional) receives a message on failure. */
 int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spin,
                     uint64_t *e_demon, double *seconds, char *err, size_t errlen);
+
+/* Per-sample run flags, active[s] != 0 = sample s runs (all, after
+ * micsa_create; NULL restores that).  A frozen sample is skipped by the
+ * sweeps, the demon walk and the measurements (its measured values read 0)
+ * and keeps its state; uploads, downloads and refreshes still act on it.
+ * Ordered with the context's queued work.  No counterpart in the reference;
+ * the batched and served runs use it for finished and empty slots. */
+int micsa_set_active(micsa_ctx *ctx, const uint8_t *active);
 
 /* Wait for all work issued on the context (cudaDeviceSynchronize,
  * main.cu:144,149) and report any asynchronous error. */

@@ -30,11 +30,13 @@ struct micsa_ctx {
   uint8_t *jb = nullptr, *lut = nullptr;
   uint32_t *te = nullptr, *keys = nullptr;
   int *walk = nullptr;
+  uint8_t *active = nullptr; /* per-sample flags, 1 = runs */
   uint64_t *stage = nullptr;
   unsigned long long *acc = nullptr;
   size_t stage_words = 0, acc_words = 0;
   int have_lut = 0;
   std::vector<int> have_j, have_spin, have_dem;
+  std::vector<uint8_t> active_host; /* host copy of the run flags */
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int64_t launches = 0;
@@ -142,6 +144,7 @@ int ensure_stage(micsa_ctx *ctx) {
 
 int ready_for_sweeps(micsa_ctx *ctx, int need_demons) {
   for (int s = 0; s < ctx->cfg.nsamples; s++) {
+    if (!ctx->active_host[s]) continue; /* frozen: never touched by the sweeps */
     if (!ctx->have_j[s] || !ctx->have_spin[s])
       return fail(ctx, MICSA_ERR_STATE, "sample %d has no couplings or spins uploaded", s);
     if (need_demons && !ctx->have_dem[s])
@@ -284,11 +287,13 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.zc = 0;
   g.pd = 0;
   g.H = s.H;
+  g.active = nullptr;
   ctx->stage_words = (size_t)s.stage_w;
   ctx->acc_words = (size_t)s.acc_w;
   ctx->have_j.assign(cfg->nsamples, 0);
   ctx->have_spin.assign(cfg->nsamples, 0);
   ctx->have_dem.assign(cfg->nsamples, 0);
+  ctx->active_host.assign(cfg->nsamples, 1);
   *out = ctx;
 #define MICSA_CK_CREATE(call)                                                  \
   do {                                                                         \
@@ -313,6 +318,9 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   MICSA_CK_CREATE(cudaMalloc(&ctx->walk, sizeof(int) * MICSA_MAX_SAMPLES));
   MICSA_CK_CREATE(cudaMalloc(&ctx->acc, 8 * ctx->acc_words));
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->walk, 0, sizeof(int) * MICSA_MAX_SAMPLES, ctx->stream));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->active, (size_t)cfg->nsamples));
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->active, 1, (size_t)cfg->nsamples, ctx->stream));
+  g.active = ctx->active;
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->spin, 0, 4 * s.spin_w, ctx->stream));
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem0, 0, 4 * s.dem_w, ctx->stream));
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem1, 0, 4 * s.dem_w, ctx->stream));
@@ -358,7 +366,8 @@ int micsa_destroy(micsa_ctx *ctx) {
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   void *bufs[] = {ctx->spin, ctx->dem0,     ctx->dem1,    ctx->rnd,      ctx->jb,
                   ctx->lut,  ctx->te,       ctx->keys,    ctx->walk,     ctx->stage,
-                  ctx->acc,  ctx->plan_lcg, ctx->plan_xo, ctx->plan_fib, ctx->rec};
+                  ctx->acc,  ctx->plan_lcg, ctx->plan_xo, ctx->plan_fib, ctx->rec,
+                  ctx->active};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -673,14 +682,16 @@ int micsa_measure(micsa_ctx *ctx, int32_t *e_spin, uint64_t *e_demon, int64_t *q
   const int64_t V = 2 * g.P;
   const unsigned long long *hu = h.data(), *hd = hu + ns * nr, *hq = hd + ns * nr,
                            *hc = hq + ns * np;
+  const std::vector<uint8_t> &on = ctx->active_host; /* frozen samples read 0 */
   for (int i = 0; i < ns * nr; i++) {
-    if (e_spin) e_spin[i] = (int32_t)(3 * V - 2 * (int64_t)hu[i]);
-    if (e_demon) e_demon[i] = hd[i];
+    if (e_spin) e_spin[i] = on[i / nr] ? (int32_t)(3 * V - 2 * (int64_t)hu[i]) : 0;
+    if (e_demon) e_demon[i] = on[i / nr] ? hd[i] : 0;
   }
   for (int i = 0; i < ns * np; i++)
-    if (q) q[i] = V - 2 * (int64_t)hq[i];
+    if (q) q[i] = on[i / np] ? V - 2 * (int64_t)hq[i] : 0;
   if (c4)
-    for (int64_t i = 0; i < (int64_t)ns * np * 3 * nd; i++) c4[i] = V - 2 * (int64_t)hc[i];
+    for (int64_t i = 0; i < (int64_t)ns * np * 3 * nd; i++)
+      c4[i] = on[i / (np * 3 * nd)] ? V - 2 * (int64_t)hc[i] : 0;
   return MICSA_OK;
 }
 
@@ -758,6 +769,24 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
   for (auto &e : ev) cudaEventDestroy(e);
   if (sweep_ms) *sweep_ms = sweep / (double)(n * per);
   if (iteration_ms) *iteration_ms = total / (double)n;
+  return MICSA_OK;
+}
+
+int micsa_set_active(micsa_ctx *ctx, const uint8_t *active) {
+  if (!ctx) return MICSA_ERR_ARG;
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  const int ns = ctx->cfg.nsamples;
+  if (!active) {
+    MICSA_CK(cudaMemsetAsync(ctx->active, 1, (size_t)ns, ctx->stream));
+    ctx->active_host.assign(ns, 1);
+    return MICSA_OK;
+  }
+  std::vector<uint8_t> a(active, active + ns);
+  for (auto &v : a) v = v ? 1 : 0;
+  ctx->active_host = a;
+  /* pageable source: returns once staged; ordered with the queued work */
+  MICSA_CK(cudaMemcpyAsync(ctx->active, a.data(), (size_t)ns, cudaMemcpyHostToDevice, ctx->stream));
   return MICSA_OK;
 }
 

@@ -273,6 +273,7 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
   const uint32_t by = blockIdx.y;
   const uint32_t tile = by % ytiles, sg = by / ytiles; /* block-uniform */
   const uint32_t s = sg / G, grp = sg % G;
+  if (micsa_frozen(g, (int)s)) return;
   const uint32_t y = tile * blockDim.y + threadIdx.y;
   if (y >= L) return;
   const uint32_t xa = 2 * (blockIdx.x * blockDim.x + threadIdx.x); /* x/2 of site A */
@@ -526,9 +527,9 @@ k_gen_rnd(const micsa_geo g, const int p, const uint32_t *__restrict__ te,
   }
 }
 
-__global__ void k_walk_advance(int *walk, int ns, int period) {
+__global__ void k_walk_advance(const micsa_geo g, int *walk, int ns, int period) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < ns) {
+  if (s < ns && !micsa_frozen(g, s)) {
     const int k = walk[s] + 1;
     walk[s] = (k == period) ? 0 : k;
   }
@@ -583,6 +584,7 @@ __global__ void __launch_bounds__(TPB)
 k_energy(const micsa_geo g, const uint32_t *__restrict__ spin, const uint8_t *__restrict__ jb,
          unsigned long long *__restrict__ unsat) {
   const int s = blockIdx.z, w = blockIdx.y, lane = threadIdx.x & 31;
+  if (micsa_frozen(g, s)) return;
   const int L = g.L, Lh = g.Lh, W = g.W;
   const int64_t P = g.P;
   const uint32_t *mine = spin + (int64_t)(s * 2) * P * W + w;
@@ -625,6 +627,7 @@ __global__ void __launch_bounds__(TPB)
 k_demon_energy(const micsa_geo g, const uint32_t *__restrict__ d0, const uint32_t *__restrict__ d1,
                unsigned long long *__restrict__ dem) {
   const int s = blockIdx.z, lane = threadIdx.x & 31;
+  if (micsa_frozen(g, s)) return;
   const int w = blockIdx.y % g.W, pi = blockIdx.y / g.W;
   const int64_t P = g.P, off = ((int64_t)s * 2 * g.nc + pi) * P * g.W + w;
   unsigned long long acc = 0;
@@ -647,6 +650,7 @@ k_overlap(const micsa_geo g, const uint32_t *__restrict__ spin, unsigned long lo
   const int nd = g.L / 2 + 1;
   const int axis = blockIdx.y / nd, dist = blockIdx.y % nd;
   const int s = blockIdx.z / g.W, w = blockIdx.z % g.W, lane = threadIdx.x & 31;
+  if (micsa_frozen(g, s)) return;
   const int L = g.L, Lh = g.Lh, W = g.W;
   const int64_t P = g.P, V = 2 * P;
   const uint32_t *sp = spin + (int64_t)(s * 2) * P * W + w;
@@ -743,7 +747,7 @@ cudaError_t micsa_launch_gen_rnd(const micsa_geo &g, int p, const uint32_t *te,
 }
 
 cudaError_t micsa_launch_walk_advance(const micsa_geo &g, int *walk, cudaStream_t st) {
-  k_walk_advance<<<(g.ns + 127) / 128, 128, 0, st>>>(walk, g.ns, g.L / 2);
+  k_walk_advance<<<(g.ns + 127) / 128, 128, 0, st>>>(g, walk, g.ns, g.L / 2);
   return cudaGetLastError();
 }
 
@@ -939,6 +943,7 @@ k_resident(const micsa_geo g, const int n, uint32_t *__restrict__ spin,
   constexpr int P = resident_cfg<L>::P, Lh = resident_cfg<L>::Lh, TPB = resident_cfg<L>::TPB;
   extern __shared__ uint4 smem_raw[];
   const int w = blockIdx.x, s = blockIdx.y, W = g.W, nc = g.nc;
+  if (micsa_frozen(g, s)) return;
   uint32_t *sp = (uint32_t *)smem_raw; /* [2][P] */
   uint32_t *sd0 = sp + 2 * P;          /* [2][nc][P] */
   uint32_t *sd1 = sd0 + 2 * nc * P;
@@ -1004,9 +1009,9 @@ k_resident(const micsa_geo g, const int n, uint32_t *__restrict__ spin,
   }
 }
 
-__global__ void k_walk_add(int *walk, int ns, int n, int period) {
+__global__ void k_walk_add(const micsa_geo g, int *walk, int ns, int n, int period) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < ns) walk[s] = (int)(((int64_t)walk[s] + n) % period);
+  if (s < ns && !micsa_frozen(g, s)) walk[s] = (int)(((int64_t)walk[s] + n) % period);
 }
 
 size_t micsa_resident_smem(int L, int nc) {
@@ -1024,7 +1029,7 @@ static cudaError_t resident_l(const micsa_geo &g, int n, uint32_t *spin, uint32_
   if (e != cudaSuccess) return e;
   k_resident<L><<<dim3(g.W, g.ns), resident_cfg<L>::TPB, bytes, st>>>(g, n, spin, d0, d1, jb, walk);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  k_walk_add<<<(g.ns + 127) / 128, 128, 0, st>>>(walk, g.ns, n, g.L / 2);
+  k_walk_add<<<(g.ns + 127) / 128, 128, 0, st>>>(g, walk, g.ns, n, g.L / 2);
   return cudaGetLastError();
 }
 

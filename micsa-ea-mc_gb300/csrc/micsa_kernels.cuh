@@ -28,7 +28,13 @@ struct micsa_geo {
   int64_t H;  /* reference words per colour, (L/4)^3/2 */
   int zc;     /* z planes per thread in the sweeps (divides L; 0 = default) */
   int pd;     /* L2 prefetch distance of the demon stream, in z steps (0 = off) */
+  const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
+                            sweeps, the walk and the measurements); null = all */
 };
+
+__host__ __device__ inline bool micsa_frozen(const micsa_geo &g, int s) {
+  return g.active && !g.active[s];
+}
 
 /* slab depths the sweep can use for this L (divisors of L, ascending) */
 int micsa_sweep_zc_candidates(int L, int *out, int max);

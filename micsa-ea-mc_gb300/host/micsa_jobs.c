@@ -38,7 +38,7 @@ static void errf(char *err, size_t n, const char *fmt, ...) {
 
 typedef struct {
   const micsa_job *jobs;
-  int j0, j1, H;
+  int j0, j1, H, NR; /* per-job buffer strides: H words, NR streams */
   uint64_t *J, *even, *odd; /* [job][12H], [job][H nr] */
   micsa_prc_t *prc;         /* [job][nr] */
   micsa_xoshiro_t *xo;
@@ -55,7 +55,7 @@ static void *init_jobs(void *arg) {
   for (int j = a->j0; j < a->j1; j++) {
     const micsa_job *jb = &a->jobs[j];
     const int L = jb->L, nr = jb->nr;
-    const int64_t V = (int64_t)L * L * L, H = a->H;
+    const int64_t V = (int64_t)L * L * L, H = a->H, NR = a->NR;
     uint64_t seed_u = micsa_check_seed(jb->seed_u);
     micsa_prc_t random_u;
     micsa_init_rand_hq(&random_u, seed_u);
@@ -70,14 +70,15 @@ static void *init_jobs(void *arg) {
     micsa_seeds_from_one(&seed_u, seeds, MAXNSAMPLES_REF * nr);
     for (int r = 0; r < nr; r++) {
       uint32_t key;
-      micsa_init_cpu_generators(&a->prc[(int64_t)j * nr + r], &a->xo[(int64_t)j * nr + r], &key,
+      micsa_init_cpu_generators(&a->prc[(int64_t)j * NR + r], &a->xo[(int64_t)j * NR + r], &key,
                                 seeds[r]);
     }
     const int list[MAXNSAMPLES_REF + 1] = {0, 0, 0};
     if (micsa_init_spins(&random_u, L, nr, MAXNSAMPLES_REF, list, 1, uu)) a->rc = MICSA_ERR_ARG;
-    micsa_pack_spins(L, nr, uu, a->even + (int64_t)j * H * nr, a->odd + (int64_t)j * H * nr);
+    micsa_pack_spins(L, nr, uu, a->even + (int64_t)j * H * NR, a->odd + (int64_t)j * H * NR);
     micsa_init_couplings_janus(jb->seed_J, L, jx, jx + V, jx + 2 * V);
     micsa_pack_couplings(L, jx, jx + V, jx + 2 * V, a->J + (int64_t)j * 12 * H);
+    (void)nr;
     free(seeds), free(uu), free(jx);
   }
   return NULL;
@@ -89,37 +90,154 @@ static double now_s(void) {
   return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
 }
 
+static int is_pow2(int64_t t) { return t > 0 && !(t & (t - 1)); }
+
+/* One shape group (same L, nr, nc, beta) in its own context and stream:
+ * jobs sorted by iterations, longest first, so the running jobs are always
+ * the slots [0, nrun). */
+typedef struct {
+  int device, n;
+  const micsa_job *jobs; /* all jobs */
+  int *idx;              /* this group's jobs, longest first */
+  const int64_t *off;    /* output offsets of every job */
+  int64_t SH, SNR;       /* strides of the per-job host buffers (words, streams) */
+  uint64_t *J, *even, *odd;
+  micsa_prc_t *prc;
+  micsa_xoshiro_t *xo;
+  int32_t *e_spin;
+  uint64_t *e_demon;
+  int rc;
+  char err[256];
+} group_run;
+
+static void *run_group(void *arg) {
+  group_run *gr = (group_run *)arg;
+  const micsa_job *j0 = &gr->jobs[gr->idx[0]];
+  const int L = j0->L, nr = j0->nr, n = gr->n;
+  micsa_config cfg = {gr->device, L, nr, n, j0->nc};
+  micsa_ctx *ctx = NULL;
+  micsa_prc_t *prc = (micsa_prc_t *)malloc(sizeof(micsa_prc_t) * nr * n);
+  micsa_xoshiro_t *xo = (micsa_xoshiro_t *)malloc(sizeof(micsa_xoshiro_t) * nr * n);
+  int32_t *es = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * nr);
+  uint64_t *ed = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n * nr);
+  uint8_t *on = (uint8_t *)malloc((size_t)n);
+  int64_t *m = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+  int rc = MICSA_OK;
+  if (!prc || !xo || !es || !ed || !on || !m) {
+    rc = MICSA_ERR_NOMEM;
+    snprintf(gr->err, sizeof gr->err, "host memory for a group of %d jobs", n);
+    goto out;
+  }
+  if ((rc = micsa_create(&cfg, &ctx))) {
+    snprintf(gr->err, sizeof gr->err, "micsa_create L=%d nr=%d n=%d failed (%d)", L, nr, n, rc);
+    goto out;
+  }
+#define CK(call)                                                                   \
+  do {                                                                             \
+    if ((rc = (call))) {                                                           \
+      snprintf(gr->err, sizeof gr->err, "%s: %s", #call, micsa_last_error(ctx));   \
+      goto out;                                                                    \
+    }                                                                              \
+  } while (0)
+  for (int k = 0; k < n; k++) {
+    const int j = gr->idx[k];
+    memcpy(prc + (int64_t)k * nr, gr->prc + (int64_t)j * gr->SNR, sizeof(micsa_prc_t) * nr);
+    memcpy(xo + (int64_t)k * nr, gr->xo + (int64_t)j * gr->SNR, sizeof(micsa_xoshiro_t) * nr);
+    CK(micsa_upload_couplings(ctx, k, gr->J + (int64_t)j * 12 * gr->SH));
+    CK(micsa_upload_spins(ctx, k, gr->even + (int64_t)j * gr->SH * gr->SNR,
+                          gr->odd + (int64_t)j * gr->SH * gr->SNR));
+    on[k] = 1;
+  }
+  {
+    uint64_t thr[3];
+    micsa_thresholds(j0->beta, thr);
+    int nrun = n;
+    int64_t t = 0;
+    while (nrun > 0) {
+      /* the host advance of the streams overlaps the iterations that follow */
+      if (!(t & (t - 1))) CK(micsa_refresh_demons_async(ctx, 0, nrun, prc, xo, thr));
+      int64_t next = 1;
+      while (next <= t) next <<= 1;
+      const int64_t last = gr->jobs[gr->idx[nrun - 1]].iterations; /* shortest running */
+      if (next > last) next = last;
+      CK(micsa_iterate(ctx, next - t));
+      t = next;
+      int any = 0;
+      for (int k = 0; k < nrun; k++) any |= is_pow2(t) || t == gr->jobs[gr->idx[k]].iterations;
+      if (!any) continue;
+      CK(micsa_measure(ctx, es, ed, NULL, NULL));
+      int still = nrun;
+      for (int k = 0; k < nrun; k++) {
+        const int j = gr->idx[k];
+        const int64_t it = gr->jobs[j].iterations;
+        if (!(is_pow2(t) || t == it)) continue;
+        const int64_t o = gr->off[j] + m[k]++ * nr;
+        if (gr->e_spin) memcpy(gr->e_spin + o, es + (int64_t)k * nr, 4 * (size_t)nr);
+        if (gr->e_demon) memcpy(gr->e_demon + o, ed + (int64_t)k * nr, 8 * (size_t)nr);
+        if (t == it) {
+          on[k] = 0;
+          still--;
+        }
+      }
+      if (still != nrun) {
+        nrun = still; /* finished jobs are the tail (longest first) */
+        CK(micsa_set_active(ctx, on));
+      }
+    }
+    CK(micsa_refresh_wait(ctx));
+    CK(micsa_synchronize(ctx));
+  }
+#undef CK
+out:
+  micsa_destroy(ctx);
+  free(prc), free(xo), free(es), free(ed), free(on), free(m);
+  gr->rc = rc;
+  return NULL;
+}
+
+static int same_group(const micsa_job *a, const micsa_job *b) {
+  return a->L == b->L && a->nr == b->nr && a->nc == b->nc && a->beta == b->beta;
+}
+
 int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spin,
                     uint64_t *e_demon, double *seconds, char *err, size_t errlen) {
-  if (!jobs || njobs < 1 || njobs > MICSA_MAX_SAMPLES)
-    return errf(err, errlen, "need 1..%d jobs", MICSA_MAX_SAMPLES), MICSA_ERR_ARG;
-  const micsa_job *j0 = &jobs[0];
-  for (int j = 1; j < njobs; j++)
-    if (jobs[j].L != j0->L || jobs[j].nr != j0->nr || jobs[j].nc != j0->nc ||
-        jobs[j].iterations != j0->iterations || jobs[j].beta != j0->beta)
-      return errf(err, errlen, "job %d: a batch runs one shape (L, nr, nc, iterations, beta)", j),
+  if (!jobs || njobs < 1) return errf(err, errlen, "need at least one job"), MICSA_ERR_ARG;
+  for (int j = 0; j < njobs; j++) {
+    micsa_config c = {device, jobs[j].L, jobs[j].nr, 1, jobs[j].nc};
+    if (micsa_footprint_bytes(&c) < 0 || jobs[j].iterations < 1)
+      return errf(err, errlen, "job %d: invalid shape L=%d nr=%d nc=%d iterations=%lld", j,
+                  jobs[j].L, jobs[j].nr, jobs[j].nc, (long long)jobs[j].iterations),
              MICSA_ERR_ARG;
-  if (j0->iterations < 1) return errf(err, errlen, "iterations must be >= 1"), MICSA_ERR_ARG;
-  micsa_config cfg = {device, j0->L, j0->nr, njobs, j0->nc};
-  if (micsa_footprint_bytes(&cfg) < 0)
-    return errf(err, errlen, "invalid shape L=%d nr=%d nc=%d", j0->L, j0->nr, j0->nc),
-           MICSA_ERR_ARG;
-  const int L = j0->L, nr = j0->nr;
-  const int64_t H = micsa_half_words(L);
-
-  /* host initialisation of every job, in parallel */
-  uint64_t *J = (uint64_t *)malloc(sizeof(uint64_t) * 12 * H * njobs);
-  uint64_t *even = (uint64_t *)malloc(sizeof(uint64_t) * H * nr * njobs);
-  uint64_t *odd = (uint64_t *)malloc(sizeof(uint64_t) * H * nr * njobs);
-  micsa_prc_t *prc = (micsa_prc_t *)malloc(sizeof(micsa_prc_t) * nr * njobs);
-  micsa_xoshiro_t *xo = (micsa_xoshiro_t *)malloc(sizeof(micsa_xoshiro_t) * nr * njobs);
-  int rc = MICSA_OK;
-  micsa_ctx *ctx = NULL;
-  if (!J || !even || !odd || !prc || !xo) {
+  }
+  /* output offsets; per-job host buffers are sized for the largest shape */
+  int64_t *off = (int64_t *)malloc(sizeof(int64_t) * (size_t)njobs);
+  int64_t maxH = 1, maxnr = 32;
+  if (!off) return errf(err, errlen, "host memory"), MICSA_ERR_NOMEM;
+  for (int j = 0, o = 0; j < njobs; j++) {
+    off[j] = o;
+    o += (int)(micsa_job_measurements(jobs[j].iterations) * jobs[j].nr);
+    const int64_t H = micsa_half_words(jobs[j].L);
+    if (H > maxH) maxH = H;
+    if (jobs[j].nr > maxnr) maxnr = jobs[j].nr;
+  }
+  uint64_t *J = (uint64_t *)malloc(sizeof(uint64_t) * 12 * maxH * njobs);
+  uint64_t *even = (uint64_t *)malloc(sizeof(uint64_t) * maxH * maxnr * njobs);
+  uint64_t *odd = (uint64_t *)malloc(sizeof(uint64_t) * maxH * maxnr * njobs);
+  micsa_prc_t *prc = (micsa_prc_t *)malloc(sizeof(micsa_prc_t) * maxnr * njobs);
+  micsa_xoshiro_t *xo = (micsa_xoshiro_t *)malloc(sizeof(micsa_xoshiro_t) * maxnr * njobs);
+  int *idx = (int *)malloc(sizeof(int) * (size_t)njobs);
+  int *gstart = (int *)malloc(sizeof(int) * ((size_t)njobs + 1));
+  group_run *grs = (group_run *)calloc((size_t)njobs, sizeof(group_run));
+  pthread_t *tid = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)njobs);
+  int *spawned = (int *)calloc((size_t)njobs, sizeof(int));
+  int rc = MICSA_OK, ng = 0;
+  if (!J || !even || !odd || !prc || !xo || !idx || !gstart || !grs || !tid || !spawned) {
     rc = MICSA_ERR_NOMEM;
     errf(err, errlen, "host memory for %d jobs", njobs);
     goto done;
   }
+  /* host initialisation of every job, in parallel (job j's buffers at
+   * stride maxH words / maxnr streams) */
   {
     enum { MAXT = 64 };
     long cores = sysconf(_SC_NPROCESSORS_ONLN);
@@ -127,16 +245,16 @@ int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spi
     if (nt > MAXT) nt = MAXT;
     if (nt > njobs) nt = njobs;
     init_share sh[MAXT];
-    pthread_t tid[MAXT];
-    int spawned[MAXT];
+    pthread_t it[MAXT];
+    int sp[MAXT];
     for (int t = 0; t < nt; t++) {
-      sh[t] = (init_share){jobs, njobs * t / nt, njobs * (t + 1) / nt, (int)H, J, even, odd,
-                           prc, xo, MICSA_OK};
-      spawned[t] = t < nt - 1 && pthread_create(&tid[t], NULL, init_jobs, &sh[t]) == 0;
-      if (!spawned[t]) init_jobs(&sh[t]);
+      sh[t] = (init_share){jobs, njobs * t / nt, njobs * (t + 1) / nt, (int)maxH, (int)maxnr,
+                           J, even, odd, prc, xo, MICSA_OK};
+      sp[t] = t < nt - 1 && pthread_create(&it[t], NULL, init_jobs, &sh[t]) == 0;
+      if (!sp[t]) init_jobs(&sh[t]);
     }
     for (int t = 0; t < nt; t++) {
-      if (spawned[t]) pthread_join(tid[t], NULL);
+      if (sp[t]) pthread_join(it[t], NULL);
       if (sh[t].rc) rc = sh[t].rc;
     }
     if (rc) {
@@ -144,60 +262,52 @@ int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spi
       goto done;
     }
   }
-
+  /* groups: stable grouping by shape, each sorted longest first */
+  {
+    int n = 0;
+    char *used = (char *)calloc((size_t)njobs, 1);
+    if (!used) {
+      rc = MICSA_ERR_NOMEM;
+      goto done;
+    }
+    for (int a = 0; a < njobs; a++) {
+      if (used[a]) continue;
+      gstart[ng++] = n;
+      for (int b = a; b < njobs; b++)
+        if (!used[b] && same_group(&jobs[a], &jobs[b])) {
+          used[b] = 1;
+          idx[n++] = b;
+        }
+    }
+    gstart[ng] = n;
+    free(used);
+    for (int g = 0; g < ng; g++) /* insertion sort by iterations, descending */
+      for (int i = gstart[g] + 1; i < gstart[g + 1]; i++)
+        for (int k = i; k > gstart[g] && jobs[idx[k]].iterations > jobs[idx[k - 1]].iterations; k--) {
+          const int tmp = idx[k];
+          idx[k] = idx[k - 1];
+          idx[k - 1] = tmp;
+        }
+  }
   {
     const double t0 = now_s();
-    if ((rc = micsa_create(&cfg, &ctx))) {
-      errf(err, errlen, "micsa_create failed (%d)", rc);
-      goto done;
+    for (int g = 0; g < ng; g++) {
+      grs[g] = (group_run){device, gstart[g + 1] - gstart[g], jobs, idx + gstart[g], off, maxH,
+                           maxnr, J, even, odd, prc, xo, e_spin, e_demon, MICSA_OK, {0}};
+      spawned[g] = g < ng - 1 && pthread_create(&tid[g], NULL, run_group, &grs[g]) == 0;
+      if (!spawned[g]) run_group(&grs[g]);
     }
-#define CK(call)                                                          \
-  do {                                                                    \
-    if ((rc = (call))) {                                                  \
-      errf(err, errlen, "%s: %s", #call, micsa_last_error(ctx));          \
-      goto done;                                                          \
-    }                                                                     \
-  } while (0)
-    for (int j = 0; j < njobs; j++) {
-      CK(micsa_upload_couplings(ctx, j, J + (int64_t)j * 12 * H));
-      CK(micsa_upload_spins(ctx, j, even + (int64_t)j * H * nr, odd + (int64_t)j * H * nr));
-    }
-    uint64_t thr[3];
-    micsa_thresholds(j0->beta, thr);
-    const int64_t nm = micsa_job_measurements(j0->iterations);
-    int32_t *es = (int32_t *)malloc(sizeof(int32_t) * (size_t)njobs * nr);
-    uint64_t *ed = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)njobs * nr);
-    if (!es || !ed) {
-      free(es), free(ed);
-      rc = MICSA_ERR_NOMEM;
-      errf(err, errlen, "host memory for measurements");
-      goto done;
-    }
-    int64_t t = 0, m = 0;
-    while (t < j0->iterations) {
-      /* the host advance of the streams overlaps the iterations that follow */
-      if (!(t & (t - 1))) CK(micsa_refresh_demons_async(ctx, 0, njobs, prc, xo, thr));
-      int64_t next = 1;
-      while (next <= t) next <<= 1;
-      if (next > j0->iterations) next = j0->iterations;
-      CK(micsa_iterate(ctx, next - t));
-      t = next;
-      if (!(t & (t - 1)) || t == j0->iterations) {
-        CK(micsa_measure(ctx, es, ed, NULL, NULL));
-        for (int j = 0; j < njobs; j++) {
-          if (e_spin) memcpy(e_spin + ((int64_t)j * nm + m) * nr, es + (int64_t)j * nr, 4 * (size_t)nr);
-          if (e_demon) memcpy(e_demon + ((int64_t)j * nm + m) * nr, ed + (int64_t)j * nr, 8 * (size_t)nr);
-        }
-        m++;
+    for (int g = 0; g < ng; g++) {
+      if (spawned[g]) pthread_join(tid[g], NULL);
+      if (grs[g].rc && !rc) {
+        rc = grs[g].rc;
+        errf(err, errlen, "%s", grs[g].err);
       }
     }
-    free(es), free(ed);
-    CK(micsa_synchronize(ctx));
     if (seconds) *seconds = now_s() - t0;
-#undef CK
   }
 done:
-  micsa_destroy(ctx);
-  free(J), free(even), free(odd), free(prc), free(xo);
+  free(off), free(J), free(even), free(odd), free(prc), free(xo), free(idx), free(gstart);
+  free(grs), free(tid), free(spawned);
   return rc;
 }

@@ -24,7 +24,7 @@ ABI_SYMBOLS = [
     "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
     "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_energy_noalloc",
     "micsa_synchronize", "micsa_kernel_launches", "micsa_stream", "micsa_job_measurements",
-    "micsa_run_batch",
+    "micsa_run_batch", "micsa_set_active",
 ]
 NOALLOC_MAX_REPLICAS = 8192
 
@@ -117,6 +117,7 @@ def lib():
         "micsa_kernel_launches": (C.c_int64, [C.c_void_p]),
         "micsa_stream": (C.c_void_p, [C.c_void_p]),
         "micsa_job_measurements": (C.c_int64, [C.c_int64]),
+        "micsa_set_active": (C.c_int, [C.c_void_p, u8p]),
         "micsa_run_batch": (C.c_int, [C.c_int, C.POINTER(Job), C.c_int, i32p, u64p,
                                       C.POINTER(C.c_double), C.c_char_p, C.c_size_t]),
         # host side (micsa-ea-mc_gb300/host/micsa_host.h)
@@ -237,6 +238,11 @@ class Context:
         check(self.h, lib().micsa_refresh_demons_async(self.h, first, count, prc, xo,
                                                        _ptr(self._thr, C.c_uint64)),
               "refresh_demons_async")
+
+    def set_active(self, flags):
+        """Per-sample run flags (None: all samples run)."""
+        a = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8)
+        check(self.h, lib().micsa_set_active(self.h, _ptr(a, C.c_uint8)), "set_active")
 
     def refresh_wait(self):
         check(self.h, lib().micsa_refresh_wait(self.h), "refresh_wait")
@@ -450,18 +456,21 @@ class HostModel:
 
 def run_batch(jobs, device=0):
     """micsa_run_batch over a list of dicts (L, nr, nc, iterations, seed_J,
-    seed_u, beta); returns (e_spin [job, m, nr], e_demon [job, m, nr], seconds)."""
+    seed_u, beta); returns ([e_spin [m, nr] per job], [e_demon ...], seconds)."""
     n = len(jobs)
     arr = (Job * n)(*[Job(j["L"], j["nr"], j["nc"], j["iterations"], j["seed_J"], j["seed_u"],
                           j["beta"]) for j in jobs])
-    nm = lib().micsa_job_measurements(jobs[0]["iterations"])
-    nr = jobs[0]["nr"]
-    es = np.zeros(n * nm * nr, np.int32)
-    ed = np.zeros(n * nm * nr, np.uint64)
+    nms = [lib().micsa_job_measurements(j["iterations"]) for j in jobs]
+    sizes = [nm * j["nr"] for nm, j in zip(nms, jobs)]
+    es = np.zeros(sum(sizes), np.int32)
+    ed = np.zeros(sum(sizes), np.uint64)
     sec = C.c_double()
     err = C.create_string_buffer(512)
     rc = lib().micsa_run_batch(device, arr, n, _ptr(es, C.c_int32), _ptr(ed, C.c_uint64),
                                C.byref(sec), err, 512)
     if rc != MICSA_OK:
         raise MicsaError("micsa_run_batch: %s %s" % (STATUS.get(rc, rc), err.value.decode()))
-    return es.reshape(n, nm, nr), ed.reshape(n, nm, nr), sec.value
+    cut = np.cumsum([0] + sizes)
+    outs = [(es[a:b].reshape(nm, j["nr"]), ed[a:b].reshape(nm, j["nr"]))
+            for a, b, nm, j in zip(cut[:-1], cut[1:], nms, jobs)]
+    return [o[0] for o in outs], [o[1] for o in outs], sec.value

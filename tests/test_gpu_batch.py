@@ -23,7 +23,7 @@ def _jobs(n, L, nr, nc, iters, base):
 def test_batch_equals_jobs_run_alone(L, nr, nc, iters, n):
     jobs = _jobs(n, L, nr, nc, iters, 1000 * L)
     es, ed, _ = micsa.run_batch(jobs)
-    assert es.shape == (n, micsa.lib().micsa_job_measurements(iters), nr)
+    assert es[0].shape == (micsa.lib().micsa_job_measurements(iters), nr)
     for j in range(n):
         e1, d1, _ = micsa.run_batch([jobs[j]])
         assert np.array_equal(es[j], e1[0]) and np.array_equal(ed[j], d1[0]), j
@@ -63,9 +63,23 @@ def test_batch_job_equals_oracle_on_reference_schedule():
         assert np.array_equal(ed[j], od.astype(np.uint64)), j
 
 
-def test_batch_rejects_mixed_shapes():
+def test_batch_mixed_shapes_and_lengths_equal_alone():
+    """Uneven L, replica counts and iteration counts in one call: shape
+    groups run concurrently, jobs finish at their own lengths."""
+    shapes = [(8, 32, 37), (16, 64, 64), (24, 32, 20), (8, 32, 5), (16, 64, 9), (24, 32, 64),
+              (8, 32, 64), (40, 32, 3)]
+    jobs = [dict(L=L, nr=nr, nc=4, iterations=it, seed_J=900 + 17 * k, seed_u=55 + 3 * k, beta=BETA)
+            for k, (L, nr, it) in enumerate(shapes)]
+    es, ed, _ = micsa.run_batch(jobs)
+    for j, job in enumerate(jobs):
+        e1, d1, _ = micsa.run_batch([job])
+        assert es[j].shape == (micsa.lib().micsa_job_measurements(job["iterations"]), job["nr"])
+        assert np.array_equal(es[j], e1[0]) and np.array_equal(ed[j], d1[0]), j
+
+
+def test_batch_rejects_invalid_job():
     jobs = _jobs(2, 8, 32, 6, 4, 5)
-    jobs[1]["nc"] = 5
+    jobs[1]["L"] = 12
     with pytest.raises(micsa.MicsaError, match="ERR_ARG"):
         micsa.run_batch(jobs)
 
@@ -75,7 +89,7 @@ def test_batch_512_samples_headline_batched_shape():
     configuration, spot-checked against single runs of three jobs."""
     jobs = _jobs(512, 16, 64, 6, 1024, 20260101)
     es, ed, sec = micsa.run_batch(jobs)
-    assert sec > 0 and es.shape == (512, 11, 64)
+    assert sec > 0 and len(es) == 512 and es[0].shape == (11, 64)
     for j in (0, 255, 511):
         e1, d1, _ = micsa.run_batch([jobs[j]])
         assert np.array_equal(es[j], e1[0]) and np.array_equal(ed[j], d1[0]), j

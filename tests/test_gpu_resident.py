@@ -48,3 +48,34 @@ def test_resident_equals_half_sweep_kernels(L, nr, nc, ns):
                 assert np.array_equal(x, y), (n, s)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("L", [8, 24])
+def test_frozen_sample_keeps_state_and_others_advance(L):
+    """micsa_set_active: a frozen sample is untouched by iterations (both the
+    resident and the per-half-sweep paths), measures as 0, and the running
+    samples evolve exactly as in a context without it."""
+    nr, nc, ns = 32, 3, 3
+    rng = np.random.default_rng(L)
+    st = random_state(rng, L, nr, nc, ns)
+    a = _ctx(L, nr, ns, nc, True, st)
+    before = a.download_spins(1) + a.download_demons(1)
+    a.set_active([1, 0, 1])
+    a.iterate(7)
+    m = a.measure()
+    assert (m["e_spin"][1] == 0).all() and (m["e_demon"][1] == 0).all()
+    for x, y in zip(before, a.download_spins(1) + a.download_demons(1)):
+        assert np.array_equal(x, y)
+    b = _ctx(L, nr, 2, nc, True, [st[0], st[2]])
+    b.iterate(7)
+    mb = b.measure()
+    assert np.array_equal(m["e_spin"][[0, 2]], mb["e_spin"])
+    assert np.array_equal(m["e_demon"][[0, 2]], mb["e_demon"])
+    for sa, sb in ((0, 0), (2, 1)):
+        for x, y in zip(a.download_spins(sa) + a.download_demons(sa),
+                        b.download_spins(sb) + b.download_demons(sb)):
+            assert np.array_equal(x, y)
+    a.set_active(None)
+    a.iterate(1)
+    a.close()
+    b.close()
