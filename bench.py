@@ -47,8 +47,11 @@ def parse():
     ap.add_argument("--nsamples", type=int, default=None,
                     help="samples (plain, default 2) or jobs (batched, default 512)")
     ap.add_argument("--nc", type=int, default=6)
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched"],
-                    help="plain: the headline run; batched: --nsamples jobs per context")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served"],
+                    help="plain: the headline run; batched: --nsamples jobs; served: a "
+                         "Poisson request stream")
+    ap.add_argument("--requests", type=int, default=200, help="served: requests in the trace")
+    ap.add_argument("--hbm-gb", type=float, default=48.0, help="served: HBM budget (GiB)")
     ap.add_argument("--iterations", type=int, default=4096,
                     help="batched with --batch-L: iterations per job")
     ap.add_argument("--batch-L", type=int, default=None,
@@ -460,9 +463,92 @@ def run_batched(a, dist):
             "pairs": {"L%d_%d" % k: v for k, v in sorted(count.items())}}
 
 
+SERVE_L = (16, 24, 32, 48, 64, 96)
+
+
+def served_trace(a):
+    """Poisson arrivals (mean 200 requests/s, seed 7); per request L uniform in
+    SERVE_L, 32 or 64 replicas, sweeps log-uniform in [2^10, 2^16], its own
+    coupling and spin seeds."""
+    rng = np.random.default_rng(7)
+    t, out = 0.0, []
+    for _ in range(a.requests):
+        t += rng.exponential(1.0 / 200.0)
+        out.append(dict(arrival=t, L=int(rng.choice(SERVE_L)), nr=int(rng.choice([32, 64])),
+                        nc=a.nc, iterations=int(round(2.0 ** rng.uniform(10.0, 16.0))),
+                        seed_J=int(rng.integers(1, 2 ** 62)), seed_u=int(rng.integers(1, 2 ** 62)),
+                        beta=BETA))
+    return out
+
+
+def run_served(a, dist):
+    """The trace through micsa_serve (continuous batching, HBM budget), in
+    real time; against the plain path: one micsa_run_batch call per request,
+    first come first served, service times from a per-(L, nr) linear fit of
+    single-job runs at 2^10 and 2^14 iterations."""
+    import micsa
+    reqs = served_trace(a)
+    budget = int(a.hbm_gb * (1 << 30))
+    micsa.serve([dict(r, arrival=0.0, iterations=8) for r in reqs[:6]], device=dist.local)
+    es, ed, times, sec = micsa.serve(reqs, device=dist.local, hbm_budget=budget)
+    lat = np.array([t[2] - r["arrival"] for t, r in zip(times, reqs)])
+    wait = np.array([t[1] - r["arrival"] for t, r in zip(times, reqs)])
+    attempts = sum(float(r["L"] ** 3) * r["nr"] * r["nc"] * r["iterations"] for r in reqs)
+    fit = {}
+    for L in SERVE_L:
+        for nr in (32, 64):
+            job = dict(L=L, nr=nr, nc=a.nc, seed_J=11, seed_u=13, beta=BETA)
+            _, _, t1 = micsa.run_batch([dict(job, iterations=1 << 10)], device=dist.local)
+            _, _, t2 = micsa.run_batch([dict(job, iterations=1 << 14)], device=dist.local)
+            b = (t2 - t1) / ((1 << 14) - (1 << 10))
+            fit[(L, nr)] = (t1 - b * (1 << 10), b)
+    free_at, plat = 0.0, []
+    for r in reqs:
+        c0, c1 = fit[(r["L"], r["nr"])]
+        start = max(r["arrival"], free_at)
+        free_at = start + c0 + c1 * r["iterations"]
+        plat.append(free_at - r["arrival"])
+    plat = np.array(plat)
+    return {"anneals_per_s": round(len(reqs) / sec, 3),
+            "p50_latency_s": round(float(np.percentile(lat, 50)), 3),
+            "p99_latency_s": round(float(np.percentile(lat, 99)), 3),
+            "p50_wait_s": round(float(np.percentile(wait, 50)), 3),
+            "attempts_per_ps": round(attempts / (sec * 1e12), 4), "seconds": round(sec, 3),
+            "arrival_window_s": round(reqs[-1]["arrival"], 3),
+            "plain_anneals_per_s": round(len(reqs) / free_at, 3),
+            "plain_p50_latency_s": round(float(np.percentile(plat, 50)), 3),
+            "plain_p99_latency_s": round(float(np.percentile(plat, 99)), 3),
+            "speedup_vs_plain": round(free_at / sec, 2),
+            "plain_fit_s": {"L%d_nr%d" % k: [round(v[0], 4), round(v[1] * 1e6, 3)]
+                            for k, v in fit.items()},
+            "hbm_budget_gib": a.hbm_gb}
+
+
 def main():
     a = parse()
     dist = Dist()
+    if a.workload == "served":
+        if a.impl == "reference" or dist.rank != 0:
+            if dist.rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "served workload: timed on "
+                                  "the GPU arm only"}))
+            dist.close()
+            return
+        r = run_served(a, dist)
+        print(json.dumps({
+            "metric": "anneals/s, served Poisson stream", "unit": "anneals/s",
+            "value": r["anneals_per_s"], "n_gpus": 1, "steps": a.requests, "warmup": 1,
+            "ms_per_step": round(r["seconds"] * 1e3 / a.requests, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic: Poisson trace, 200 requests/s, seed 7, per-request seeds",
+            "config": {"workload": "served: %d requests, L uniform in %s, 32/64 replicas, sweeps "
+                                   "log-uniform in [2^10, 2^16], nc=%d, continuous batching "
+                                   "under a %g GiB HBM budget" % (a.requests, list(SERVE_L), a.nc,
+                                                                  a.hbm_gb),
+                       "requests": a.requests, "nc": a.nc},
+            "detail": r}))
+        dist.close()
+        return
     if a.workload == "batched":
         if a.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "batched workload: timed on the "

@@ -212,6 +212,38 @@ int64_t micsa_job_measurements(int64_t iterations);
 int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spin,
                     uint64_t *e_demon, double *seconds, char *err, size_t errlen);
 
+/* ---- Serving: no counterpart in the reference ----
+ * Anneal requests (jobs) arrive over time and are continuously batched: per
+ * shape (L, nr, nc, beta) one context of S sample slots on its own stream
+ * and host thread, S chosen so that all shapes' contexts fit hbm_budget; a
+ * request is initialised on host threads once it has arrived, admitted into
+ * the next free slot, runs its own reference schedule (refresh at its own
+ * t = 0 and powers of two, measurements at powers of two and at the end)
+ * in rounds shared with the other slots, and leaves its slot to the next
+ * request when done.  Results equal the job run alone (micsa_run_batch). */
+typedef struct {
+  double arrival;  /* seconds after the start of the run */
+  micsa_job job;
+} micsa_request;
+typedef struct {
+  double prepared, admitted, finished; /* seconds after the start; latency = finished - arrival */
+} micsa_request_result;
+typedef struct {
+  int device;
+  int64_t hbm_budget;  /* bytes all contexts may hold together (0: 48 GiB) */
+  int slots_max;       /* slots per shape (0: 64) */
+  int64_t chunk;       /* most iterations per round (0: 1024) */
+  int prep_threads;    /* host threads initialising requests (0: cores - 1) */
+} micsa_serve_config;
+/* Replay n requests in real time (request j becomes visible at its arrival
+ * time after the start; contexts are created before the start).  Outputs as
+ * micsa_run_batch's (offsets over the requests in the given order); res[j]
+ * receives the request's times; seconds (optional) the time of the last
+ * finish. */
+int micsa_serve(const micsa_serve_config *cfg, const micsa_request *req, int n,
+                micsa_request_result *res, int32_t *e_spin, uint64_t *e_demon, double *seconds,
+                char *err, size_t errlen);
+
 /* Per-sample run flags, active[s] != 0 = sample s runs (all, after
  * micsa_create; NULL restores that).  A frozen sample is skipped by the
  * sweeps, the demon walk and the measurements (its measured values read 0)

@@ -17,7 +17,7 @@ LIB = os.path.join(PKG, "lib")
 BIN = os.path.join(PKG, "bin")
 
 HOST_C = ["host/micsa_rng.c", "host/micsa_model.c", "host/micsa_io.c", "host/micsa_jump.c",
-          "host/micsa_jobs.c"]
+          "host/micsa_jobs.c", "host/micsa_serve.c"]
 CUDA = ["csrc/micsa_kernels.cu", "csrc/micsa_api.cu", "csrc/micsa_noalloc.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -24,7 +24,7 @@ ABI_SYMBOLS = [
     "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
     "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_energy_noalloc",
     "micsa_synchronize", "micsa_kernel_launches", "micsa_stream", "micsa_job_measurements",
-    "micsa_run_batch", "micsa_set_active",
+    "micsa_run_batch", "micsa_set_active", "micsa_serve",
 ]
 NOALLOC_MAX_REPLICAS = 8192
 
@@ -56,6 +56,19 @@ class Job(C.Structure):
     """micsa_job (include/micsa.h): one reference run of one sample."""
     _fields_ = [("L", C.c_int), ("nr", C.c_int), ("nc", C.c_int), ("iterations", C.c_int64),
                 ("seed_J", C.c_uint64), ("seed_u", C.c_uint64), ("beta", C.c_double)]
+
+
+class Request(C.Structure):
+    _fields_ = [("arrival", C.c_double), ("job", Job)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("prepared", C.c_double), ("admitted", C.c_double), ("finished", C.c_double)]
+
+
+class ServeConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget", C.c_int64), ("slots_max", C.c_int),
+                ("chunk", C.c_int64), ("prep_threads", C.c_int)]
 
 
 class RefreshPlan(C.Structure):
@@ -118,6 +131,9 @@ def lib():
         "micsa_stream": (C.c_void_p, [C.c_void_p]),
         "micsa_job_measurements": (C.c_int64, [C.c_int64]),
         "micsa_set_active": (C.c_int, [C.c_void_p, u8p]),
+        "micsa_serve": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(Request), C.c_int,
+                                  C.POINTER(RequestResult), i32p, u64p, C.POINTER(C.c_double),
+                                  C.c_char_p, C.c_size_t]),
         "micsa_run_batch": (C.c_int, [C.c_int, C.POINTER(Job), C.c_int, i32p, u64p,
                                       C.POINTER(C.c_double), C.c_char_p, C.c_size_t]),
         # host side (micsa-ea-mc_gb300/host/micsa_host.h)
@@ -474,3 +490,29 @@ def run_batch(jobs, device=0):
     outs = [(es[a:b].reshape(nm, j["nr"]), ed[a:b].reshape(nm, j["nr"]))
             for a, b, nm, j in zip(cut[:-1], cut[1:], nms, jobs)]
     return [o[0] for o in outs], [o[1] for o in outs], sec.value
+
+
+def serve(requests, device=0, hbm_budget=0, slots_max=0, chunk=0, prep_threads=0):
+    """micsa_serve over a list of dicts (arrival + the job fields); returns
+    (e_spin per request, e_demon per request, [(prepared, admitted,
+    finished)], seconds)."""
+    n = len(requests)
+    arr = (Request * n)(*[Request(r["arrival"], Job(r["L"], r["nr"], r["nc"], r["iterations"],
+                                                    r["seed_J"], r["seed_u"], r["beta"]))
+                          for r in requests])
+    nms = [lib().micsa_job_measurements(r["iterations"]) for r in requests]
+    sizes = [nm * r["nr"] for nm, r in zip(nms, requests)]
+    es = np.zeros(sum(sizes), np.int32)
+    ed = np.zeros(sum(sizes), np.uint64)
+    res = (RequestResult * n)()
+    cfg = ServeConfig(device, hbm_budget, slots_max, chunk, prep_threads)
+    sec = C.c_double()
+    err = C.create_string_buffer(512)
+    rc = lib().micsa_serve(C.byref(cfg), arr, n, res, _ptr(es, C.c_int32), _ptr(ed, C.c_uint64),
+                           C.byref(sec), err, 512)
+    if rc != MICSA_OK:
+        raise MicsaError("micsa_serve: %s %s" % (STATUS.get(rc, rc), err.value.decode()))
+    cut = np.cumsum([0] + sizes)
+    e_s = [es[a:b].reshape(nm, r["nr"]) for a, b, nm, r in zip(cut[:-1], cut[1:], nms, requests)]
+    e_d = [ed[a:b].reshape(nm, r["nr"]) for a, b, nm, r in zip(cut[:-1], cut[1:], nms, requests)]
+    return e_s, e_d, [(x.prepared, x.admitted, x.finished) for x in res], sec.value
