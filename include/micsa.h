@@ -190,7 +190,12 @@ typedef struct {
   uint64_t seed_J;     /* coupling seed */
   uint64_t seed_u;     /* spin / demon-stream seed (0: drawn from /dev/urandom) */
   double beta;         /* demon temperature (beta.in) */
+  double beta_end;     /* 0 or beta: constant; else the refresh at iteration t draws
+                          at beta + (beta_end - beta) * t / iterations (a linear
+                          schedule; the reference has one beta, NBETAS = 1) */
 } micsa_job;
+/* The inverse temperature a job's refresh at iteration t uses. */
+double micsa_job_beta(const micsa_job *job, int64_t t);
 /* Measurement points of a job: t = 1, 2, 4, ... <= iterations, plus
  * iterations itself when it is not a power of two. */
 int64_t micsa_job_measurements(int64_t iterations);
@@ -214,7 +219,7 @@ int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spi
 
 /* ---- Serving: no counterpart in the reference ----
  * Anneal requests (jobs) arrive over time and are continuously batched: per
- * shape (L, nr, nc, beta) one context of S sample slots on its own stream
+ * shape (L, nr, nc) one context of S sample slots on its own stream
  * and host thread, S chosen so that all shapes' contexts fit hbm_budget; a
  * request is initialised on host threads once it has arrived, admitted into
  * the next free slot, runs its own reference schedule (refresh at its own

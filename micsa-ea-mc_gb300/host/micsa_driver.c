@@ -15,7 +15,8 @@
  * directory is "{dir}I%03d/" as io.c:661 intends (the reference formats it
  * with overlapping sprintf buffers); changentimes.in is parsed as "count
  * then times" (io.c:930-968 reads through an uninitialised pointer).
- * Setting MICSA_OBSERVABLES=1 also writes evol_q.txt and evol_C4.txt.
+ * Setting MICSA_OBSERVABLES=1 also writes evol_q.txt, evol_C4.txt and evol_xi.txt
+ * (correlation lengths xi12, xi23 from C4).
  */
 #define _GNU_SOURCE
 #include <errno.h>
@@ -595,6 +596,13 @@ static void write_measures(unsigned long long ib, const int64_t *q, const int64_
             for (int a = 0; a < 3; a++) s += c4[(((int64_t)b * np + k) * 3 + a) * nd + d];
           fprintf(f, "%llu %d %lld\n", ib, d, s);
         }
+        fclose(f);
+      }
+      snprintf(name, sizeof name, "%sevol_xi.txt", dirsample[b]);
+      if ((f = fopen(name, "a"))) {
+        double x12, x23;
+        micsa_correlation_lengths(M.L, np, c4 + (int64_t)b * np * 3 * nd, NULL, &x12, &x23);
+        fprintf(f, "%llu %14.10g %14.10g\n", ib, x12, x23);
         fclose(f);
       }
     }

@@ -161,6 +161,13 @@ void micsa_energy_stats(const int32_t *e_spin, int nr, int L, double *mean,
 void micsa_demon_stats(const uint64_t *e_demon, int nr, int L, int nc,
                        double *mean, double *std);
 
+/* ---- observables beyond the reference ----
+ * c4[(k*3 + axis)*(L/2+1) + d] of npairs replica pairs (micsa_measure's
+ * layout for one sample) -> C4r[d] (pair- and axis-averaged, / V; may be
+ * NULL) and the integral-estimator correlation lengths xi12, xi23 */
+void micsa_correlation_lengths(int L, int npairs, const int64_t *c4, double *C4r,
+                               double *xi12, double *xi23);
+
 #ifdef __cplusplus
 }
 #endif

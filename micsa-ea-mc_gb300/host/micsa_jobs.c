@@ -21,6 +21,13 @@
 
 #define MAXNSAMPLES_REF 2 /* header.h:20, sizes the reference's seed fan-out */
 
+double micsa_job_beta(const micsa_job *job, int64_t t) {
+  if (job->beta_end == 0 || job->beta_end == job->beta || job->iterations < 1) return job->beta;
+  return job->beta + (job->beta_end - job->beta) * (double)t / (double)job->iterations;
+}
+
+static int has_schedule(const micsa_job *j) { return j->beta_end != 0 && j->beta_end != j->beta; }
+
 int64_t micsa_job_measurements(int64_t iterations) {
   if (iterations < 1) return 0;
   int64_t n = 0, p = 1;
@@ -155,7 +162,17 @@ static void *run_group(void *arg) {
     int64_t t = 0;
     while (nrun > 0) {
       /* the host advance of the streams overlaps the iterations that follow */
-      if (!(t & (t - 1))) CK(micsa_refresh_demons_async(ctx, 0, nrun, prc, xo, thr));
+      if (!(t & (t - 1))) {
+        if (!has_schedule(j0)) {
+          CK(micsa_refresh_demons_async(ctx, 0, nrun, prc, xo, thr));
+        } else { /* each job at its own point of its beta schedule */
+          for (int k = 0; k < nrun; k++) {
+            uint64_t tk[3];
+            micsa_thresholds(micsa_job_beta(&gr->jobs[gr->idx[k]], t), tk);
+            CK(micsa_refresh_demons_async(ctx, k, 1, prc + (int64_t)k * nr, xo + (int64_t)k * nr, tk));
+          }
+        }
+      }
       int64_t next = 1;
       while (next <= t) next <<= 1;
       const int64_t last = gr->jobs[gr->idx[nrun - 1]].iterations; /* shortest running */
@@ -196,7 +213,8 @@ out:
 }
 
 static int same_group(const micsa_job *a, const micsa_job *b) {
-  return a->L == b->L && a->nr == b->nr && a->nc == b->nc && a->beta == b->beta;
+  return a->L == b->L && a->nr == b->nr && a->nc == b->nc && a->beta == b->beta &&
+         has_schedule(a) == has_schedule(b) && (!has_schedule(a) || a->beta_end == b->beta_end);
 }
 
 int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spin,

@@ -338,3 +338,27 @@ void micsa_demon_stats(const uint64_t *e_demon, int nr, int L, int nc,
   *mean = a;
   *std = sqrt(s);
 }
+
+/* Correlation lengths from C4 by the integral estimators of the Janus
+ * collaboration (Belletti et al., Phys. Rev. Lett. 101, 157201 (2008)):
+ * I_k = sum_{r=0}^{L/2} r^k C4(r), xi_{k,k+1} = I_{k+1} / I_k, with C4(r)
+ * the pair- and axis-averaged correlation normalised by V.  The sums run
+ * over the whole range (no noise cut-off). */
+void micsa_correlation_lengths(int L, int npairs, const int64_t *c4, double *C4r,
+                               double *xi12, double *xi23) {
+  const int nd = L / 2 + 1;
+  const double V = (double)L * L * L, norm = 1.0 / (V * 3.0 * (double)npairs);
+  double I1 = 0, I2 = 0, I3 = 0;
+  for (int d = 0; d < nd; d++) {
+    double s = 0;
+    for (int k = 0; k < npairs; k++)
+      for (int a = 0; a < 3; a++) s += (double)c4[((int64_t)k * 3 + a) * nd + d];
+    const double c = s * norm, r = (double)d;
+    if (C4r) C4r[d] = c;
+    I1 += r * c;
+    I2 += r * r * c;
+    I3 += r * r * r * c;
+  }
+  if (xi12) *xi12 = I1 != 0 ? I2 / I1 : 0;
+  if (xi23) *xi23 = I2 != 0 ? I3 / I2 : 0;
+}

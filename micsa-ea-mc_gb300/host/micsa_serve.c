@@ -2,7 +2,7 @@
  * Serving: anneal requests arriving over time, continuously batched.
  *
  * Each request is a job (one reference run, micsa_job).  Requests of one
- * shape (L, nr, nc, beta) share a pool: one context of S sample slots on its
+ * shape (L, nr, nc) share a pool: one context of S sample slots on its
  * own CUDA stream, driven by its own host thread; S is chosen so that every
  * pool of the trace fits the HBM budget.  A request is initialised on host
  * threads once it has arrived, then waits for a free slot.  A pool thread
@@ -95,7 +95,6 @@ struct server;
 typedef struct {
   struct server *sv;
   int L, nr, nc, S;
-  double beta;
   micsa_ctx *ctx;
   micsa_prc_t *prc; /* [S][nr] */
   micsa_xoshiro_t *xo;
@@ -160,8 +159,6 @@ static void *pool_thread(void *arg) {
   server *sv = pl->sv;
   const int nr = pl->nr, S = pl->S;
   const int64_t chunk = sv->cfg->chunk > 0 ? sv->cfg->chunk : 1024;
-  uint64_t thr[3];
-  micsa_thresholds(pl->beta, thr);
   int rc = MICSA_OK;
 #define CK(call)                                                                  \
   do {                                                                            \
@@ -204,8 +201,13 @@ static void *pool_thread(void *arg) {
     /* refreshes due (refresh_walkers at t = 0 and powers of two) */
     for (int k = 0; k < S; k++)
       if (pl->slot_req[k] >= 0 && (pl->slot_t[k] == 0 || is_pow2(pl->slot_t[k])))
+      {
+        /* the job's own beta at its own clock (pools mix betas) */
+        uint64_t tk[3];
+        micsa_thresholds(micsa_job_beta(&sv->req[pl->slot_req[k]].job, pl->slot_t[k]), tk);
         CK(micsa_refresh_demons_async(pl->ctx, k, 1, pl->prc + (int64_t)k * nr,
-                                      pl->xo + (int64_t)k * nr, thr));
+                                      pl->xo + (int64_t)k * nr, tk));
+      }
     /* the round: up to the nearest slot event */
     int64_t R = chunk;
     for (int k = 0; k < S; k++) {
@@ -259,7 +261,7 @@ out:
 }
 
 static int same_shape(const micsa_job *a, const micsa_job *b) {
-  return a->L == b->L && a->nr == b->nr && a->nc == b->nc && a->beta == b->beta;
+  return a->L == b->L && a->nr == b->nr && a->nc == b->nc;
 }
 
 int micsa_serve(const micsa_serve_config *cfg, const micsa_request *req, int n,
@@ -306,14 +308,13 @@ int micsa_serve(const micsa_serve_config *cfg, const micsa_request *req, int n,
     int p = 0;
     for (; p < sv.npools; p++) {
       const pool *pp = &sv.pools[p];
-      const micsa_job shape = {pp->L, pp->nr, pp->nc, 0, 0, 0, pp->beta};
+      const micsa_job shape = {pp->L, pp->nr, pp->nc, 0, 0, 0, 0, 0};
       if (same_shape(&req[j].job, &shape)) break;
     }
     if (p == sv.npools) {
       pool *pl = &sv.pools[sv.npools++];
       pl->sv = &sv;
       pl->L = req[j].job.L, pl->nr = req[j].job.nr, pl->nc = req[j].job.nc;
-      pl->beta = req[j].job.beta;
       pthread_mutex_init(&pl->mu, NULL);
       pthread_cond_init(&pl->cv, NULL);
     }

@@ -24,7 +24,7 @@ ABI_SYMBOLS = [
     "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
     "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_energy_noalloc",
     "micsa_synchronize", "micsa_kernel_launches", "micsa_stream", "micsa_job_measurements",
-    "micsa_run_batch", "micsa_set_active", "micsa_serve",
+    "micsa_run_batch", "micsa_set_active", "micsa_serve", "micsa_job_beta",
 ]
 NOALLOC_MAX_REPLICAS = 8192
 
@@ -55,7 +55,8 @@ class Xoshiro(C.Structure):
 class Job(C.Structure):
     """micsa_job (include/micsa.h): one reference run of one sample."""
     _fields_ = [("L", C.c_int), ("nr", C.c_int), ("nc", C.c_int), ("iterations", C.c_int64),
-                ("seed_J", C.c_uint64), ("seed_u", C.c_uint64), ("beta", C.c_double)]
+                ("seed_J", C.c_uint64), ("seed_u", C.c_uint64), ("beta", C.c_double),
+                ("beta_end", C.c_double)]
 
 
 class Request(C.Structure):
@@ -131,6 +132,7 @@ def lib():
         "micsa_stream": (C.c_void_p, [C.c_void_p]),
         "micsa_job_measurements": (C.c_int64, [C.c_int64]),
         "micsa_set_active": (C.c_int, [C.c_void_p, u8p]),
+        "micsa_job_beta": (C.c_double, [C.POINTER(Job), C.c_int64]),
         "micsa_serve": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(Request), C.c_int,
                                   C.POINTER(RequestResult), i32p, u64p, C.POINTER(C.c_double),
                                   C.c_char_p, C.c_size_t]),
@@ -152,6 +154,8 @@ def lib():
                                             C.c_int, C.c_int, u64p, u64p, C.c_int]),
         "micsa_fill_bits": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), C.c_int, C.c_uint64,
                                    C.c_int, C.c_uint32, u32p]),
+        "micsa_correlation_lengths": (None, [C.c_int, C.c_int, i64p, C.POINTER(C.c_double),
+                                             C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "micsa_draw_demons": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), u64p, C.c_int, C.c_int,
                                      C.c_int, C.c_int, u64p, u64p]),
         # jump-ahead of the refresh streams (micsa-ea-mc_gb300/host/micsa_jump.h)
@@ -475,7 +479,7 @@ def run_batch(jobs, device=0):
     seed_u, beta); returns ([e_spin [m, nr] per job], [e_demon ...], seconds)."""
     n = len(jobs)
     arr = (Job * n)(*[Job(j["L"], j["nr"], j["nc"], j["iterations"], j["seed_J"], j["seed_u"],
-                          j["beta"]) for j in jobs])
+                          j["beta"], j.get("beta_end", 0.0)) for j in jobs])
     nms = [lib().micsa_job_measurements(j["iterations"]) for j in jobs]
     sizes = [nm * j["nr"] for nm, j in zip(nms, jobs)]
     es = np.zeros(sum(sizes), np.int32)
@@ -498,7 +502,8 @@ def serve(requests, device=0, hbm_budget=0, slots_max=0, chunk=0, prep_threads=0
     finished)], seconds)."""
     n = len(requests)
     arr = (Request * n)(*[Request(r["arrival"], Job(r["L"], r["nr"], r["nc"], r["iterations"],
-                                                    r["seed_J"], r["seed_u"], r["beta"]))
+                                                    r["seed_J"], r["seed_u"], r["beta"],
+                                                    r.get("beta_end", 0.0)))
                           for r in requests])
     nms = [lib().micsa_job_measurements(r["iterations"]) for r in requests]
     sizes = [nm * r["nr"] for nm, r in zip(nms, requests)]
@@ -516,3 +521,15 @@ def serve(requests, device=0, hbm_budget=0, slots_max=0, chunk=0, prep_threads=0
     e_s = [es[a:b].reshape(nm, r["nr"]) for a, b, nm, r in zip(cut[:-1], cut[1:], nms, requests)]
     e_d = [ed[a:b].reshape(nm, r["nr"]) for a, b, nm, r in zip(cut[:-1], cut[1:], nms, requests)]
     return e_s, e_d, [(x.prepared, x.admitted, x.finished) for x in res], sec.value
+
+
+def correlation_lengths(L, c4):
+    """(C4(r) averaged over pairs and axes / V, xi12, xi23) from one sample's
+    c4 array [pairs, 3, L/2+1] (micsa_measure's layout)."""
+    c = np.ascontiguousarray(c4, dtype=np.int64)
+    npairs = c.size // (3 * (L // 2 + 1))
+    out = np.zeros(L // 2 + 1, np.float64)
+    x12, x23 = C.c_double(), C.c_double()
+    lib().micsa_correlation_lengths(L, npairs, _ptr(c, C.c_int64), _ptr(out, C.c_double),
+                                    C.byref(x12), C.byref(x23))
+    return out, x12.value, x23.value

@@ -93,3 +93,36 @@ def test_batch_512_samples_headline_batched_shape():
     for j in (0, 255, 511):
         e1, d1, _ = micsa.run_batch([jobs[j]])
         assert np.array_equal(es[j], e1[0]) and np.array_equal(ed[j], d1[0]), j
+
+
+def test_batch_beta_schedule_equals_alone_and_oracle():
+    """Linear beta schedule (an extension: the reference has one beta): each
+    refresh draws the demons at beta(t); the batch equals the jobs alone and
+    the oracle with the thresholds recomputed at every refresh."""
+    jobs = [dict(L=8, nr=32, nc=6, iterations=it, seed_J=31 + k, seed_u=41 + k, beta=0.1,
+                 beta_end=1.5) for k, it in enumerate((40, 17, 40))]
+    es, ed, _ = micsa.run_batch(jobs)
+    for j, job in enumerate(jobs):
+        e1, d1, _ = micsa.run_batch([job])
+        assert np.array_equal(es[j], e1[0]) and np.array_equal(ed[j], d1[0]), j
+    job = jobs[0]
+    L, nr, nc = job["L"], job["nr"], job["nc"]
+    hm = micsa.HostModel(L, nr, nc, 1, job["seed_u"], [1] * nr, [0], beta=job["beta"])
+    J = micsa.pack_couplings(L, *micsa.couplings_janus(job["seed_J"], L)[:3])
+    even, odd = hm.spins[0][0].copy(), hm.spins[0][1].copy()
+    out, t = [], 0
+    while t < job["iterations"]:
+        if t & (t - 1) == 0:
+            b = job["beta"] + (job["beta_end"] - job["beta"]) * t / job["iterations"]
+            hm.thr = micsa.thresholds(b)
+            w0, w1 = hm.draw_demons(0)
+        nxt = 1
+        while nxt <= t:
+            nxt <<= 1
+        nxt = min(nxt, job["iterations"])
+        for _ in range(nxt - t):
+            oracle.micsa_iteration(L, nr, nc, J, even, odd, w0, w1, 8)
+        t = nxt
+        if t & (t - 1) == 0 or t == job["iterations"]:
+            out.append(oracle.demon_energy(L, nr, nc, w0, w1))
+    assert np.array_equal(ed[0], np.array(out).astype(np.uint64))
