@@ -144,10 +144,11 @@ int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0,
 int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration_ms);
 
 /* Text line describing the launch shape the context's autotuner chose at
- * creation: "zc=<z planes per thread> pd=<prefetch distance> | <zc>/<pd>:<ms
- * per half-sweep> ...".  The environment variables MICSA_SWEEP_ZC and
- * MICSA_SWEEP_PD, read by micsa_create, pin the shape and skip the timing
- * (no candidates listed then).  The reference has fixed launch geometry
+ * creation: "zc=<z planes per thread> pd=<prefetch distance> split=<0: one
+ * launch for all samples, 1: one per sample> | <zc>/<pd>/<split>:<ms per
+ * half-sweep> ...".  The environment variables MICSA_SWEEP_ZC, MICSA_SWEEP_PD
+ * and MICSA_SWEEP_SPLIT, read by micsa_create, pin the shape and skip the
+ * timing (no candidates listed then).  The reference has fixed launch geometry
  * (calculate_blocks, ini.c:580-602). */
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n);
 

@@ -20,7 +20,7 @@
 #include "micsa_jump.h"
 #include "micsa_kernels.cuh"
 
-#define MICSA_TUNE_MAX 24
+#define MICSA_TUNE_MAX 48
 
 struct micsa_ctx {
   micsa_config cfg;
@@ -41,8 +41,11 @@ struct micsa_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   int64_t launches = 0;
   int resident = 0;        /* small lattice: iterations run in shared memory */
+  int split = 0;           /* 1: one half-sweep launch per sample (smaller L2 working set) */
+  int64_t graph_launches = 0; /* kernels per replay of the iteration graph */
   int ntune = 0;           /* launch shapes timed at creation */
   int tune_zc[MICSA_TUNE_MAX] = {0}, tune_pd[MICSA_TUNE_MAX] = {0};
+  int tune_split[MICSA_TUNE_MAX] = {0};
   double tune_ms[MICSA_TUNE_MAX] = {0};
   /* demon refresh on the device: jump tables of one segment length */
   micsa_refresh_plan plan = {};
@@ -173,6 +176,45 @@ void parallel_for(int64_t n, int64_t grain, F f) {
   for (auto &th : pool) th.join();
 }
 
+/* One micSA half-sweep: of every sample in one launch (s < 0), or of sample
+ * s alone -- the launch then sees only that sample's spins, couplings and
+ * demon planes through offset pointers. */
+cudaError_t launch_half(micsa_ctx *ctx, const micsa_geo &g, int s, int p, int ic,
+                        int64_t *launches) {
+  if (launches) ++*launches;
+  if (s < 0)
+    return micsa_launch_sweep_micsa(g, p, ic, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb, ctx->walk,
+                                    ctx->stream);
+  const size_t PW = (size_t)g.P * g.W;
+  micsa_geo g1 = g;
+  g1.ns = 1;
+  g1.active = g.active ? g.active + s : nullptr; /* a frozen sample returns at once */
+  return micsa_launch_sweep_micsa(g1, p, ic, ctx->spin + s * 2 * PW,
+                                  ctx->dem0 + s * 2 * (size_t)g.nc * PW,
+                                  ctx->dem1 + s * 2 * (size_t)g.nc * PW,
+                                  ctx->jb + (size_t)s * 2 * g.P, ctx->walk + s, ctx->stream);
+}
+
+/* The half-sweeps of one iteration (ic = ic0 .. ic1-1).  split = 0: plane by
+ * plane, all samples per launch.  split = 1: sample-major, all of sample 0's
+ * half-sweeps, then sample 1's, ...: the spins that stay hot in L2 across
+ * consecutive launches are one sample's. */
+cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0, int ic1,
+                          int64_t *launches) {
+  cudaError_t e = cudaSuccess;
+  if (!split) {
+    for (int ic = ic0; ic < ic1; ic++)
+      for (int p = 0; p < 2; p++)
+        if ((e = launch_half(ctx, g, -1, p, ic, launches)) != cudaSuccess) return e;
+    return e;
+  }
+  for (int s = 0; s < g.ns; s++)
+    for (int ic = ic0; ic < ic1; ic++)
+      for (int p = 0; p < 2; p++)
+        if ((e = launch_half(ctx, g, s, p, ic, launches)) != cudaSuccess) return e;
+  return e;
+}
+
 /* Slab-depth autotuner: time a (colour 0, colour 1) pair of micSA
  * half-sweeps for every z-chunk length that divides L, on the freshly zeroed
  * buffers, keep the fastest, then zero the buffers again.  Results do not
@@ -196,6 +238,8 @@ int autotune(micsa_ctx *ctx) {
                   zc, pd, g.L);
     g.zc = zc;
     g.pd = pd;
+    const char *es = getenv("MICSA_SWEEP_SPLIT");
+    ctx->split = es && atoi(es) && g.ns > 1;
     ctx->ntune = 0;
     return MICSA_OK;
   }
@@ -203,8 +247,9 @@ int autotune(micsa_ctx *ctx) {
   MICSA_CK(cudaEventCreate(&e0));
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
-  int best_zc = zcs[nz - 1], best_pd = 0, n = 0;
+  int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, n = 0;
   const int reps = 4;
+  for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
   for (int c = 0; c < nz; c++)
     for (int d = 0; d < 3; d++) {
       if (pds[d] && pds[d] >= zcs[c]) continue; /* prefetch only within a slab */
@@ -212,9 +257,7 @@ int autotune(micsa_ctx *ctx) {
       g.pd = pds[d];
       for (int rep = -1; rep < reps; rep++) { /* rep -1: warm-up */
         if (rep == 0) MICSA_CK(cudaEventRecord(e0, ctx->stream));
-        for (int p = 0; p < 2; p++)
-          MICSA_CK(micsa_launch_sweep_micsa(g, p, 0, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
-                                            ctx->walk, ctx->stream));
+        MICSA_CK(launch_halves(ctx, g, sp, 0, 1, nullptr));
       }
       MICSA_CK(cudaEventRecord(e1, ctx->stream));
       MICSA_CK(cudaEventSynchronize(e1));
@@ -224,6 +267,7 @@ int autotune(micsa_ctx *ctx) {
       if (n < MICSA_TUNE_MAX) {
         ctx->tune_zc[n] = g.zc;
         ctx->tune_pd[n] = g.pd;
+        ctx->tune_split[n] = sp;
         ctx->tune_ms[n] = per;
         n++;
       }
@@ -231,23 +275,24 @@ int autotune(micsa_ctx *ctx) {
         best = per;
         best_zc = g.zc;
         best_pd = g.pd;
+        best_split = sp;
       }
     }
   ctx->ntune = n;
   g.zc = best_zc;
   g.pd = best_pd;
+  ctx->split = best_split;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return MICSA_OK;
 }
 
-int enqueue_micsa_iteration(micsa_ctx *ctx) {
+/* one iteration's launches; *launches counts them */
+int enqueue_micsa_iteration(micsa_ctx *ctx, int64_t *launches) {
   const micsa_geo &g = ctx->g;
-  for (int ic = 0; ic < g.nc; ic++)
-    for (int p = 0; p < 2; p++)
-      MICSA_CK(micsa_launch_sweep_micsa(g, p, ic, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
-                                        ctx->walk, ctx->stream));
+  MICSA_CK(launch_halves(ctx, g, ctx->split, 0, g.nc, launches));
   MICSA_CK(micsa_launch_walk_advance(g, ctx->walk, ctx->stream));
+  if (launches) ++*launches;
   return MICSA_OK;
 }
 
@@ -350,10 +395,10 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d pd=%d |", ctx->g.zc, ctx->g.pd);
+  int k = snprintf(buf, n, "zc=%d pd=%d split=%d |", ctx->g.zc, ctx->g.pd, ctx->split);
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
-    k += snprintf(buf + k, n - (size_t)k, " %d/%d:%.5fms", ctx->tune_zc[c], ctx->tune_pd[c],
-                  ctx->tune_ms[c]);
+    k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d:%.5fms", ctx->tune_zc[c], ctx->tune_pd[c],
+                  ctx->tune_split[c], ctx->tune_ms[c]);
   return MICSA_OK;
 }
 
@@ -607,8 +652,9 @@ int micsa_monte_carlo(micsa_ctx *ctx, int flag, const uint32_t *te, const uint32
   const micsa_geo &g = ctx->g;
   if (flag == 1) {
     if ((rc = ready_for_sweeps(ctx, 1))) return rc;
-    if ((rc = enqueue_micsa_iteration(ctx))) return rc;
-    ctx->launches += 2 * g.nc + 1;
+    int64_t nl = 0;
+    if ((rc = enqueue_micsa_iteration(ctx, &nl))) return rc;
+    ctx->launches += nl;
     return MICSA_OK;
   }
   if (flag != 0) return fail(ctx, MICSA_ERR_ARG, "flag must be 0 or 1, got %d", flag);
@@ -632,7 +678,8 @@ int micsa_iterate(micsa_ctx *ctx, int64_t n) {
   if (rc || (rc = ready_for_sweeps(ctx, 1))) return rc;
   if (!ctx->graph_exec && !ctx->resident) {
     MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    rc = enqueue_micsa_iteration(ctx);
+    ctx->graph_launches = 0;
+    rc = enqueue_micsa_iteration(ctx, &ctx->graph_launches);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
     if (rc) {
@@ -655,7 +702,7 @@ int micsa_iterate(micsa_ctx *ctx, int64_t n) {
     return MICSA_OK;
   }
   for (int64_t i = 0; i < n; i++) MICSA_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
-  ctx->launches += n * (2 * ctx->g.nc + 1);
+  ctx->launches += n * ctx->graph_launches;
   return MICSA_OK;
 }
 
@@ -748,15 +795,14 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
   for (auto &e : ev) MICSA_CK(cudaEventCreate(&e));
   MICSA_CK(cudaEventRecord(ev[0], ctx->stream));
   for (int64_t it = 0; it < n; it++) {
-    for (int ic = 0; ic < g.nc; ic++)
-      for (int p = 0; p < 2; p++)
-        MICSA_CK(micsa_launch_sweep_micsa(g, p, ic, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
-                                          ctx->walk, ctx->stream));
+    int64_t nl = 0;
+    MICSA_CK(launch_halves(ctx, g, ctx->split, 0, g.nc, &nl));
+    ctx->launches += nl;
     MICSA_CK(cudaEventRecord(ev[2 * it + 1], ctx->stream));
     MICSA_CK(micsa_launch_walk_advance(g, ctx->walk, ctx->stream));
     MICSA_CK(cudaEventRecord(ev[2 * it + 2], ctx->stream));
   }
-  ctx->launches += n * (per + 1);
+  ctx->launches += n;
   MICSA_CK(cudaStreamSynchronize(ctx->stream));
   double sweep = 0, total = 0;
   for (int64_t it = 0; it < n; it++) {
