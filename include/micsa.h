@@ -145,10 +145,11 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
 
 /* Text line describing the launch shape the context's autotuner chose at
  * creation: "zc=<z planes per thread> pd=<prefetch distance> split=<0: one
- * launch for all samples, 1: one per sample> | <zc>/<pd>/<split>:<ms per
- * half-sweep> ...".  The environment variables MICSA_SWEEP_ZC, MICSA_SWEEP_PD
- * and MICSA_SWEEP_SPLIT, read by micsa_create, pin the shape and skip the
- * timing (no candidates listed then).  The reference has fixed launch geometry
+ * launch for all samples, 1: sample-major, one launch per sample>
+ * occ=<blocks per SM the registers are allocated for> | <zc>/<pd>/<split>/
+ * <occ>:<ms per half-sweep> ...".  The environment variables MICSA_SWEEP_ZC,
+ * MICSA_SWEEP_PD, MICSA_SWEEP_SPLIT and MICSA_SWEEP_OCC, read by micsa_create,
+ * pin the shape and skip the timing (no candidates listed then).  The reference has fixed launch geometry
  * (calculate_blocks, ini.c:580-602). */
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n);
 

@@ -20,7 +20,7 @@
 #include "micsa_jump.h"
 #include "micsa_kernels.cuh"
 
-#define MICSA_TUNE_MAX 48
+#define MICSA_TUNE_MAX 64
 
 struct micsa_ctx {
   micsa_config cfg;
@@ -45,7 +45,7 @@ struct micsa_ctx {
   int64_t graph_launches = 0; /* kernels per replay of the iteration graph */
   int ntune = 0;           /* launch shapes timed at creation */
   int tune_zc[MICSA_TUNE_MAX] = {0}, tune_pd[MICSA_TUNE_MAX] = {0};
-  int tune_split[MICSA_TUNE_MAX] = {0};
+  int tune_split[MICSA_TUNE_MAX] = {0}, tune_occ[MICSA_TUNE_MAX] = {0};
   double tune_ms[MICSA_TUNE_MAX] = {0};
   /* demon refresh on the device: jump tables of one segment length */
   micsa_refresh_plan plan = {};
@@ -215,9 +215,10 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
   return e;
 }
 
-/* Slab-depth autotuner: time a (colour 0, colour 1) pair of micSA
- * half-sweeps for every z-chunk length that divides L, on the freshly zeroed
- * buffers, keep the fastest, then zero the buffers again.  Results do not
+/* Launch-shape autotuner: time the half-sweeps of whole iterations, in their
+ * real launch order, for every z-chunk length that divides L, prefetch
+ * distance, sample order (merged or sample-major) and register budget, on the
+ * freshly zeroed buffers; keep the fastest, then zero the buffers again.  Results do not
  * depend on the choice (each site is updated by exactly one thread either
  * way); only the speed does. */
 int autotune(micsa_ctx *ctx) {
@@ -238,8 +239,9 @@ int autotune(micsa_ctx *ctx) {
                   zc, pd, g.L);
     g.zc = zc;
     g.pd = pd;
-    const char *es = getenv("MICSA_SWEEP_SPLIT");
+    const char *es = getenv("MICSA_SWEEP_SPLIT"), *eo = getenv("MICSA_SWEEP_OCC");
     ctx->split = es && atoi(es) && g.ns > 1;
+    g.occ = eo && atoi(eo) == 4 ? 4 : 3;
     ctx->ntune = 0;
     return MICSA_OK;
   }
@@ -247,27 +249,31 @@ int autotune(micsa_ctx *ctx) {
   MICSA_CK(cudaEventCreate(&e0));
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
-  int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, n = 0;
-  const int reps = 4;
+  int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, n = 0;
+  const int reps = 2;
+  const int nocc = g.W % 4 ? 2 : 1; /* the 4-blocks variant exists for VW <= 2 */
+  for (int oc = 0; oc < nocc; oc++)
   for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
   for (int c = 0; c < nz; c++)
     for (int d = 0; d < 3; d++) {
       if (pds[d] && pds[d] >= zcs[c]) continue; /* prefetch only within a slab */
       g.zc = zcs[c];
       g.pd = pds[d];
+      g.occ = oc ? 4 : 3;
       for (int rep = -1; rep < reps; rep++) { /* rep -1: warm-up */
         if (rep == 0) MICSA_CK(cudaEventRecord(e0, ctx->stream));
-        MICSA_CK(launch_halves(ctx, g, sp, 0, 1, nullptr));
+        MICSA_CK(launch_halves(ctx, g, sp, 0, g.nc, nullptr)); /* one iteration's order */
       }
       MICSA_CK(cudaEventRecord(e1, ctx->stream));
       MICSA_CK(cudaEventSynchronize(e1));
       float ms = 0;
       MICSA_CK(cudaEventElapsedTime(&ms, e0, e1));
-      const double per = ms / (2.0 * reps);
+      const double per = ms / (2.0 * g.nc * reps);
       if (n < MICSA_TUNE_MAX) {
         ctx->tune_zc[n] = g.zc;
         ctx->tune_pd[n] = g.pd;
         ctx->tune_split[n] = sp;
+        ctx->tune_occ[n] = g.occ;
         ctx->tune_ms[n] = per;
         n++;
       }
@@ -276,12 +282,14 @@ int autotune(micsa_ctx *ctx) {
         best_zc = g.zc;
         best_pd = g.pd;
         best_split = sp;
+        best_occ = g.occ;
       }
     }
   ctx->ntune = n;
   g.zc = best_zc;
   g.pd = best_pd;
   ctx->split = best_split;
+  g.occ = best_occ;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return MICSA_OK;
@@ -331,6 +339,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.P = s.P;
   g.zc = 0;
   g.pd = 0;
+  g.occ = 3;
   g.H = s.H;
   g.active = nullptr;
   ctx->stage_words = (size_t)s.stage_w;
@@ -395,10 +404,11 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d pd=%d split=%d |", ctx->g.zc, ctx->g.pd, ctx->split);
+  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d |", ctx->g.zc, ctx->g.pd, ctx->split,
+                   ctx->g.occ);
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
-    k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d:%.5fms", ctx->tune_zc[c], ctx->tune_pd[c],
-                  ctx->tune_split[c], ctx->tune_ms[c]);
+    k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d:%.5fms", ctx->tune_zc[c], ctx->tune_pd[c],
+                  ctx->tune_split[c], ctx->tune_occ[c], ctx->tune_ms[c]);
   return MICSA_OK;
 }
 

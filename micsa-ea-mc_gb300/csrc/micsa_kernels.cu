@@ -261,8 +261,8 @@ template <int VW, bool WIDE> struct pairs {
  * bytes and the two demon words per plane.  Block = (TX pairs along x/2) x
  * (TY rows); TX divides L/4; grid = (L/4/TX, ytiles*ns*G, L/zc).
  * In-plane offsets are 32-bit (P*W < 2^32 is checked at creation). */
-template <int VW, bool MICSA, bool WIDE>
-__global__ void __launch_bounds__(TPB)
+template <int VW, bool MICSA, bool WIDE, int MINB>
+__global__ void __launch_bounds__(TPB, MINB)
 k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
         const int zc, const int pd, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
         uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
@@ -705,17 +705,19 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
   const int zc = g.zc > 0 ? g.zc : ((g.L >= 128 && g.L % 16 == 0) ? 16 : (g.L >= 48 ? 8 : 2));
   dim3 block(tx, ty);
   dim3 grid(g.Lh / 2 / tx, ytiles * g.ns * G, g.L / zc);
+  /* blocks per SM the register allocation is made for: the default (3, or
+   * 2 for 4-word vectors), or occ = 4 (at most 64 registers, VW <= 2) */
+  constexpr int B0 = VW == 4 ? 2 : 3, B1 = VW == 4 ? 2 : 4;
+#define MICSA_SWEEP(M, WD, B) \
+  k_sweep<VW, M, WD, B><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd)
   if (G == 1) {
-    if (micsa)
-      k_sweep<VW, true, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
-    else
-      k_sweep<VW, false, true><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
+    if (micsa) { if (g.occ == 4) MICSA_SWEEP(true, true, B1); else MICSA_SWEEP(true, true, B0); }
+    else MICSA_SWEEP(false, true, B0);
   } else {
-    if (micsa)
-      k_sweep<VW, true, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
-    else
-      k_sweep<VW, false, false><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd);
+    if (micsa) { if (g.occ == 4) MICSA_SWEEP(true, false, B1); else MICSA_SWEEP(true, false, B0); }
+    else MICSA_SWEEP(false, false, B0);
   }
+#undef MICSA_SWEEP
   return cudaGetLastError();
 }
 

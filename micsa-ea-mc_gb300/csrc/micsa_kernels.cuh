@@ -28,6 +28,7 @@ struct micsa_geo {
   int64_t H;  /* reference words per colour, (L/4)^3/2 */
   int zc;     /* z planes per thread in the sweeps (divides L; 0 = default) */
   int pd;     /* L2 prefetch distance of the demon stream, in z steps (0 = off) */
+  int occ;    /* sweep variant: 4 = register cap for 4 blocks per SM, else the compiler's */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */
 };
