@@ -197,12 +197,12 @@ def run_micsa(a, dist):
     hm = micsa.HostModel(L, nr, nc, SEEDS["seed_J"], SEEDS["seed_u"],
                          [SEEDS["seed_MC0"] + r for r in range(nr)], list(range(ns)), beta=BETA,
                          nthreads=os.cpu_count() or 8)
-    demons = [hm.draw_demons(b) for b in range(ns)]
     ctx = micsa.Context(L, nr, ns, nc, device=dev)
     for b in range(ns):
         ctx.upload_couplings(b, hm.J[b])
         ctx.upload_spins(b, *hm.spins[b])
-        ctx.upload_demons(b, *demons[b])
+        ctx.refresh_demons(b, hm.prc_C[b], hm.xo_C[b], hm.thr)  # InitWalkers on the GPU
+    demons = [ctx.download_demons(b) for b in range(ns)]  # for the upload-every-step variant
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     attempts = float(L ** 3) * nr * ns * nc
     # ---- device-resident throughput: one graph replay per step

@@ -625,7 +625,12 @@ int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, 
   MICSA_CK(cudaMemcpyAsync(ctx->rec, rec, words * sizeof(uint64_t), cudaMemcpyHostToDevice,
                            ctx->stream));
   MICSA_CK(cudaEventRecord(ctx->rec_copied, ctx->stream));
-  MICSA_CK(micsa_launch_refresh(g, first, count, nw, wps, ctx->plan.nseg, ctx->rec, ctx->plan_lcg,
+  micsa_geo gr = g;
+  {
+    const char *e = getenv("MICSA_REFRESH_OCC"); /* 1: the unconstrained-register variant */
+    gr.occ = e && atoi(e) == 1 ? 1 : 6;
+  }
+  MICSA_CK(micsa_launch_refresh(gr, first, count, nw, wps, ctx->plan.nseg, ctx->rec, ctx->plan_lcg,
                                 ctx->plan_xo, ctx->plan_fib, thr, ctx->dem0, ctx->dem1,
                                 ctx->stream));
   ctx->launches++;

@@ -831,7 +831,8 @@ __device__ __forceinline__ void xoshiro_step(uint64_t &s0, uint64_t &s1, uint64_
   s3 = rotl64(s3, 45);
 }
 
-__global__ void __launch_bounds__(64)
+template <int MINB>
+__global__ void __launch_bounds__(64, MINB)
 k_refresh(const micsa_geo g, const int first, const int count, const int64_t nwords,
           const int wps, const int64_t nseg, const uint64_t *__restrict__ rec,
           const uint64_t *__restrict__ lcg, const uint64_t *__restrict__ xoq,
@@ -915,9 +916,14 @@ cudaError_t micsa_launch_refresh(const micsa_geo &g, int first, int count, int64
                                  const uint64_t *xoq, const uint64_t *fib, const uint64_t thr[3],
                                  uint32_t *dem0, uint32_t *dem1, cudaStream_t st) {
   const int64_t warps = (int64_t)count * g.W * nseg;
-  k_refresh<<<(unsigned)((warps + 1) / 2), 64, 0, st>>>(g, first, count, nwords, wps, nseg, rec,
-                                                        lcg, xoq, fib, thr[0], thr[1], thr[2],
-                                                        dem0, dem1);
+  const unsigned blocks = (unsigned)((warps + 1) / 2);
+  /* registers for 6 blocks (12 warps) per SM: 168, with a small spill */
+  if (g.occ == 1)
+    k_refresh<1><<<blocks, 64, 0, st>>>(g, first, count, nwords, wps, nseg, rec, lcg, xoq, fib,
+                                        thr[0], thr[1], thr[2], dem0, dem1);
+  else
+    k_refresh<6><<<blocks, 64, 0, st>>>(g, first, count, nwords, wps, nseg, rec, lcg, xoq, fib,
+                                        thr[0], thr[1], thr[2], dem0, dem1);
   return cudaGetLastError();
 }
 
