@@ -280,8 +280,8 @@ def e2e_job(a, dist, ctx, hm, attempts):
     lib = micsa.lib()
 
     def job():
-        prc = [(micsa.PRC * nr).from_buffer_copy(start[b][0]) for b in range(ns)]
-        xo = [(micsa.Xoshiro * nr).from_buffer_copy(start[b][1]) for b in range(ns)]
+        prc = (micsa.PRC * (ns * nr)).from_buffer_copy(b"".join(x[0] for x in start))
+        xo = (micsa.Xoshiro * (ns * nr)).from_buffer_copy(b"".join(x[1] for x in start))
         for b in range(ns):
             micsa.check(ctx.h, lib.micsa_upload_couplings(ctx.h, b, p64(J[b][1])), "couplings")
             micsa.check(ctx.h, lib.micsa_upload_spins(ctx.h, b, p64(sp[b][0][1]), p64(sp[b][1][1])),
@@ -289,8 +289,14 @@ def e2e_job(a, dist, ctx, hm, attempts):
         t, nref, nmeas = 0, 0, 0
         while t < a.steps:
             if t & (t - 1) == 0:
-                for b in range(ns):
-                    ctx.refresh_demons(b, prc[b], xo[b], hm.thr)
+                # refresh t was drawn ahead (t > 0); draw the next one during
+                # the iterations that follow (side stream)
+                if t == 0:
+                    ctx.refresh_demons_async(0, prc, xo, hm.thr)
+                else:
+                    ctx.refresh_commit()
+                if (2 * t if t else 1) < a.steps:
+                    ctx.refresh_demons_ahead(0, prc, xo, hm.thr)
                 nref += 1
             nxt = 1
             while nxt <= t:
@@ -301,6 +307,7 @@ def e2e_job(a, dist, ctx, hm, attempts):
             if t & (t - 1) == 0 or t == a.steps:
                 ctx.measure(spin=True, demon=True)
                 nmeas += 1
+        ctx.refresh_wait()
         for b in range(ns):
             o = outs[b]
             micsa.check(ctx.h, lib.micsa_download_spins(ctx.h, b, p64(o[0][1]), p64(o[1][1])), "spins")
@@ -321,8 +328,8 @@ def e2e_job(a, dist, ctx, hm, attempts):
             "h2d_bytes_per_step": int(h2d // a.steps), "d2h_bytes_per_step": int(d2h // a.steps),
             "ms_per_step": round(te * 1e3 / a.steps, 4), "job_ms": round(te * 1e3, 2),
             "refreshes": nref, "measurements": nmeas,
-            "step": "job of `steps` iterations: state upload, GPU demon refresh + energy readback "
-                    "at t=0,1,2,4,..., final spins+demons readback"}
+            "step": "job of `steps` iterations: state upload, GPU demon refresh (drawn ahead on a "
+                    "side stream) + energy readback at t=0,1,2,4,..., final spins+demons readback"}
 
 
 def e2e_upload_every_step(a, dist, ctx, demons, attempts):

@@ -100,6 +100,17 @@ int micsa_refresh_demons(micsa_ctx *ctx, int first, int count, void *prc, void *
 int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
                                const uint64_t *thr);
 int micsa_refresh_wait(micsa_ctx *ctx);
+/* The next refresh drawn ahead: as micsa_refresh_demons_async, but the
+ * demons go into a back buffer (allocated on first use, the size of the
+ * demon planes) on a side stream, so the draw overlaps the iterations queued
+ * on the context's stream -- the GPU form of the reference's background
+ * InitWalkers thread (main.cu:340-377).  micsa_refresh_commit makes them
+ * current (ordered after the draw and after the work already queued: a
+ * device copy, and the walks of those samples reset).  One refresh may be
+ * pending at a time.  No counterpart in the reference. */
+int micsa_refresh_demons_ahead(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
+                               const uint64_t *thr);
+int micsa_refresh_commit(micsa_ctx *ctx);
 
 /* One iteration of Monte_Carlo (main.cu:197-313) on all samples.
  *   flag = 1: nc x (even, odd) microcanonical half-sweeps, then the demon
@@ -136,11 +147,12 @@ int micsa_download_spins(micsa_ctx *ctx, int sample, uint64_t *even,
 int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0,
                           uint64_t *w1);
 
-/* Run n microcanonical iterations with CUDA events around each iteration's
- * back-to-back half-sweeps and around its walk, and report the mean device
- * time of one half-sweep launch and of one whole iteration, in milliseconds
- * (the per-kernel view of measure_time, timing.c:3-33).  Advances the state
- * like micsa_iterate. */
+/* Run n microcanonical iterations, each a replay of the iteration's CUDA
+ * graph (as micsa_iterate runs it) with event nodes around its half-sweeps
+ * and around its walk, and report the mean device time of one half-sweep
+ * (of all samples) and of one whole iteration, in milliseconds (the
+ * per-kernel view of measure_time, timing.c:3-33).  Advances the state like
+ * micsa_iterate. */
 int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration_ms);
 
 /* Text line describing the launch shape the context's autotuner chose at

@@ -53,6 +53,14 @@ struct micsa_ctx {
   uint64_t *rec = nullptr, *rec_host = nullptr; /* start records: device, pinned staging */
   size_t rec_words = 0;
   cudaEvent_t rec_copied = nullptr;  /* staging upload done */
+  /* refresh drawn ahead into a back buffer on a side stream */
+  cudaStream_t side = nullptr;
+  uint32_t *back0 = nullptr, *back1 = nullptr;
+  uint64_t *rec_b = nullptr;
+  size_t rec_b_words = 0;
+  cudaEvent_t ahead_done = nullptr;  /* the draw into the back buffer is done */
+  cudaEvent_t commit_done = nullptr; /* the back buffer has been copied out */
+  int ahead_first = 0, ahead_count = 0; /* pending drawn-ahead samples (count 0: none) */
   std::thread advancer;              /* host advance of the last refresh's streams */
   char err[512] = {0};
 };
@@ -360,7 +368,12 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
     }                                                                          \
   } while (0)
   MICSA_CK_CREATE(cudaSetDevice(cfg->device));
-  MICSA_CK_CREATE(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  {
+    /* highest priority: work drawn ahead on the side stream yields to it */
+    int least = 0, greatest = 0;
+    MICSA_CK_CREATE(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    MICSA_CK_CREATE(cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, greatest));
+  }
   MICSA_CK_CREATE(cudaMalloc(&ctx->spin, 4 * s.spin_w));
   MICSA_CK_CREATE(cudaMalloc(&ctx->dem0, 4 * s.dem_w));
   MICSA_CK_CREATE(cudaMalloc(&ctx->dem1, 4 * s.dem_w));
@@ -415,7 +428,16 @@ int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
 int micsa_destroy(micsa_ctx *ctx) {
   if (!ctx) return MICSA_OK;
   if (ctx->advancer.joinable()) ctx->advancer.join();
-  cudaSetDevice(ctx->cfg.device);
+  if (ctx->side) {
+    cudaSetDevice(ctx->cfg.device);
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamDestroy(ctx->side);
+  }
+  if (ctx->back0) cudaFree(ctx->back0);
+  if (ctx->back1) cudaFree(ctx->back1);
+  if (ctx->rec_b) cudaFree(ctx->rec_b);
+  if (ctx->ahead_done) cudaEventDestroy(ctx->ahead_done);
+  if (ctx->commit_done) cudaEventDestroy(ctx->commit_done);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
@@ -544,6 +566,7 @@ namespace {
 int ensure_refresh_plan(micsa_ctx *ctx, int64_t nw, int wps) {
   if (ctx->plan.lcg && ctx->plan.nwords == nw && ctx->plan.words_per_seg == wps) return MICSA_OK;
   MICSA_CK(cudaStreamSynchronize(ctx->stream)); /* the old tables may still be read */
+  if (ctx->side) MICSA_CK(cudaStreamSynchronize(ctx->side));
   micsa_refresh_plan_free(&ctx->plan);
   for (uint64_t **b : {&ctx->plan_lcg, &ctx->plan_xo, &ctx->plan_fib}) {
     if (*b) cudaFree(*b);
@@ -570,8 +593,13 @@ int micsa_refresh_wait(micsa_ctx *ctx) {
   return MICSA_OK;
 }
 
-int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
-                               const uint64_t *thr) {
+namespace {
+
+/* One refresh of samples first .. first+count-1: drawn on the context's
+ * stream into the current demons (ahead = 0), or on the side stream into
+ * the back buffer (ahead = 1, made current by micsa_refresh_commit). */
+int refresh_into(micsa_ctx *ctx, int first, int count, void *prc, void *xo, const uint64_t *thr,
+                 int ahead) {
   if (!ctx || !prc || !xo || !thr) return fail(ctx, MICSA_ERR_ARG, "null argument");
   if (first < 0 || count < 1 || first + count > ctx->cfg.nsamples)
     return fail(ctx, MICSA_ERR_ARG, "samples [%d, %d) out of range [0, %d)", first, first + count,
@@ -579,6 +607,8 @@ int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, 
   micsa_refresh_wait(ctx); /* the previous refresh's structs may be these */
   int rc = set_device(ctx);
   if (rc) return rc;
+  if (ahead && ctx->ahead_count)
+    return fail(ctx, MICSA_ERR_STATE, "a refresh drawn ahead is not committed yet");
   const micsa_geo &g = ctx->g;
   micsa_prc_t *P = (micsa_prc_t *)prc;
   micsa_xoshiro_t *X = (micsa_xoshiro_t *)xo;
@@ -593,6 +623,7 @@ int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, 
   if (ctx->rec_copied) MICSA_CK(cudaEventSynchronize(ctx->rec_copied));
   if (ctx->rec_words < words) {
     MICSA_CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->side) MICSA_CK(cudaStreamSynchronize(ctx->side));
     if (ctx->rec) cudaFree(ctx->rec);
     if (ctx->rec_host) cudaFreeHost(ctx->rec_host);
     ctx->rec = ctx->rec_host = nullptr;
@@ -601,6 +632,33 @@ int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, 
     MICSA_CK(cudaHostAlloc(&ctx->rec_host, words * sizeof(uint64_t), cudaHostAllocDefault));
     ctx->rec_words = words;
   }
+  if (ahead) {
+    const size_t dw = (size_t)ctx->cfg.nsamples * 2 * g.nc * g.P * g.W;
+    if (!ctx->side) {
+      /* the draw ahead fills what the sweeps leave idle: lowest priority */
+      int least = 0, greatest = 0;
+      MICSA_CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      MICSA_CK(cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, least));
+    }
+    if (!ctx->ahead_done)
+      MICSA_CK(cudaEventCreateWithFlags(&ctx->ahead_done, cudaEventDisableTiming));
+    if (!ctx->commit_done)
+      MICSA_CK(cudaEventCreateWithFlags(&ctx->commit_done, cudaEventDisableTiming));
+    /* the last commit's copy out of the back buffer must have run */
+    MICSA_CK(cudaStreamWaitEvent(ctx->side, ctx->commit_done, 0));
+    if (!ctx->back0) MICSA_CK(cudaMalloc(&ctx->back0, 4 * dw));
+    if (!ctx->back1) MICSA_CK(cudaMalloc(&ctx->back1, 4 * dw));
+    if (ctx->rec_b_words < words) {
+      MICSA_CK(cudaStreamSynchronize(ctx->side));
+      if (ctx->rec_b) cudaFree(ctx->rec_b);
+      ctx->rec_b = nullptr;
+      ctx->rec_b_words = 0;
+      MICSA_CK(cudaMalloc(&ctx->rec_b, words * sizeof(uint64_t)));
+      ctx->rec_b_words = words;
+    }
+  }
+  cudaStream_t st = ahead ? ctx->side : ctx->stream;
+  uint64_t *drec = ahead ? ctx->rec_b : ctx->rec;
   if (!ctx->rec_copied) MICSA_CK(cudaEventCreateWithFlags(&ctx->rec_copied, cudaEventDisableTiming));
 
   /* start records, grouped by warp, built in parallel; checked before
@@ -622,20 +680,25 @@ int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, 
     return fail(ctx, MICSA_ERR_ARG, "stream %lld: PR ring pointers are not 24, 55, 61 apart",
                 (long long)bad.load());
   if ((rc = ensure_refresh_plan(ctx, nw, wps))) return rc;
-  MICSA_CK(cudaMemcpyAsync(ctx->rec, rec, words * sizeof(uint64_t), cudaMemcpyHostToDevice,
-                           ctx->stream));
-  MICSA_CK(cudaEventRecord(ctx->rec_copied, ctx->stream));
+  MICSA_CK(cudaMemcpyAsync(drec, rec, words * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+  MICSA_CK(cudaEventRecord(ctx->rec_copied, st));
   micsa_geo gr = g;
   {
     const char *e = getenv("MICSA_REFRESH_OCC"); /* 1: the unconstrained-register variant */
     gr.occ = e && atoi(e) == 1 ? 1 : 6;
   }
-  MICSA_CK(micsa_launch_refresh(gr, first, count, nw, wps, ctx->plan.nseg, ctx->rec, ctx->plan_lcg,
-                                ctx->plan_xo, ctx->plan_fib, thr, ctx->dem0, ctx->dem1,
-                                ctx->stream));
+  MICSA_CK(micsa_launch_refresh(gr, first, count, nw, wps, ctx->plan.nseg, drec, ctx->plan_lcg,
+                                ctx->plan_xo, ctx->plan_fib, thr, ahead ? ctx->back0 : ctx->dem0,
+                                ahead ? ctx->back1 : ctx->dem1, st));
   ctx->launches++;
-  MICSA_CK(cudaMemsetAsync(ctx->walk + first, 0, count * sizeof(int), ctx->stream));
-  for (int s = first; s < first + count; s++) ctx->have_dem[s] = 1;
+  if (ahead) {
+    MICSA_CK(cudaEventRecord(ctx->ahead_done, ctx->side));
+    ctx->ahead_first = first;
+    ctx->ahead_count = count;
+  } else {
+    MICSA_CK(cudaMemsetAsync(ctx->walk + first, 0, count * sizeof(int), ctx->stream));
+    for (int s = first; s < first + count; s++) ctx->have_dem[s] = 1;
+  }
 
   /* the caller's streams move past the draws on host threads while the
    * device draws (and runs whatever is queued next) */
@@ -650,6 +713,39 @@ int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, 
   } catch (...) {
     advance();
   }
+  return MICSA_OK;
+}
+
+}  // namespace
+
+int micsa_refresh_demons_async(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
+                               const uint64_t *thr) {
+  return refresh_into(ctx, first, count, prc, xo, thr, 0);
+}
+
+int micsa_refresh_demons_ahead(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
+                               const uint64_t *thr) {
+  return refresh_into(ctx, first, count, prc, xo, thr, 1);
+}
+
+int micsa_refresh_commit(micsa_ctx *ctx) {
+  if (!ctx) return MICSA_ERR_ARG;
+  if (!ctx->ahead_count) return fail(ctx, MICSA_ERR_STATE, "no refresh drawn ahead");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  const micsa_geo &g = ctx->g;
+  const size_t per = 2 * (size_t)g.nc * g.P * g.W; /* words per sample and plane type */
+  const size_t off = (size_t)ctx->ahead_first * per, n = (size_t)ctx->ahead_count * per;
+  MICSA_CK(cudaStreamWaitEvent(ctx->stream, ctx->ahead_done, 0));
+  MICSA_CK(cudaMemcpyAsync(ctx->dem0 + off, ctx->back0 + off, 4 * n, cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+  MICSA_CK(cudaMemcpyAsync(ctx->dem1 + off, ctx->back1 + off, 4 * n, cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+  MICSA_CK(cudaEventRecord(ctx->commit_done, ctx->stream));
+  MICSA_CK(cudaMemsetAsync(ctx->walk + ctx->ahead_first, 0, ctx->ahead_count * sizeof(int),
+                           ctx->stream));
+  for (int s = ctx->ahead_first; s < ctx->ahead_first + ctx->ahead_count; s++) ctx->have_dem[s] = 1;
+  ctx->ahead_count = 0;
   return MICSA_OK;
 }
 
@@ -804,30 +900,40 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
   if (rc || (rc = ready_for_sweeps(ctx, 1))) return rc;
   const micsa_geo &g = ctx->g;
   const int per = 2 * g.nc;
-  /* events around each iteration's half-sweeps (issued back to back, as in
-   * the graph) and around its walk */
-  std::vector<cudaEvent_t> ev((size_t)(2 * n + 1));
+  /* one iteration as a CUDA graph, as micsa_iterate runs it, with event
+   * nodes before the half-sweeps, between them and the walk, and after it;
+   * each replay is read back before the next */
+  cudaEvent_t ev[3];
   for (auto &e : ev) MICSA_CK(cudaEventCreate(&e));
-  MICSA_CK(cudaEventRecord(ev[0], ctx->stream));
-  for (int64_t it = 0; it < n; it++) {
-    int64_t nl = 0;
-    MICSA_CK(launch_halves(ctx, g, ctx->split, 0, g.nc, &nl));
-    ctx->launches += nl;
-    MICSA_CK(cudaEventRecord(ev[2 * it + 1], ctx->stream));
-    MICSA_CK(micsa_launch_walk_advance(g, ctx->walk, ctx->stream));
-    MICSA_CK(cudaEventRecord(ev[2 * it + 2], ctx->stream));
-  }
-  ctx->launches += n;
-  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t nl = 0;
   double sweep = 0, total = 0;
-  for (int64_t it = 0; it < n; it++) {
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    e = cudaEventRecordWithFlags(ev[0], ctx->stream, cudaEventRecordExternal);
+    if (e == cudaSuccess) e = launch_halves(ctx, g, ctx->split, 0, g.nc, &nl);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[1], ctx->stream, cudaEventRecordExternal);
+    if (e == cudaSuccess) e = micsa_launch_walk_advance(g, ctx->walk, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal);
+    const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  for (int64_t it = 0; it < n && e == cudaSuccess; it++) {
+    e = cudaGraphLaunch(exec, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     float a = 0, b = 0;
-    MICSA_CK(cudaEventElapsedTime(&a, ev[2 * it], ev[2 * it + 1]));
-    MICSA_CK(cudaEventElapsedTime(&b, ev[2 * it + 1], ev[2 * it + 2]));
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&a, ev[0], ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&b, ev[1], ev[2]);
     sweep += a;
     total += a + b;
   }
-  for (auto &e : ev) cudaEventDestroy(e);
+  ctx->launches += n * (nl + 1);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  for (auto &x : ev) cudaEventDestroy(x);
+  MICSA_CK(e);
   if (sweep_ms) *sweep_ms = sweep / (double)(n * per);
   if (iteration_ms) *iteration_ms = total / (double)n;
   return MICSA_OK;

@@ -326,9 +326,14 @@ static void init_model(void) {
     micsa_init_cpu_generators(&M.random_PRC[r], &M.random_xo[r], &M.seed_keys[r], data.seed_MC[r]);
   M.seeds_C = (uint64_t *)xmalloc(8 * (size_t)MAXNSAMPLES * nr);
   micsa_seeds_from_one(&data.seed_u, M.seeds_C, MAXNSAMPLES * nr);
+  /* the samples' demon streams contiguous ([nbits][nr]): one GPU refresh
+   * call covers all samples */
+  micsa_prc_t *prc_all = (micsa_prc_t *)xmalloc(sizeof(micsa_prc_t) * nr * (M.nbits ? M.nbits : 1));
+  micsa_xoshiro_t *xo_all =
+      (micsa_xoshiro_t *)xmalloc(sizeof(micsa_xoshiro_t) * nr * (M.nbits ? M.nbits : 1));
   for (int b = 0; b < M.nbits; b++) {
-    M.random_PRC_C[b] = (micsa_prc_t *)xmalloc(sizeof(micsa_prc_t) * nr);
-    M.random_xo_C[b] = (micsa_xoshiro_t *)xmalloc(sizeof(micsa_xoshiro_t) * nr);
+    M.random_PRC_C[b] = prc_all + (int64_t)b * nr;
+    M.random_xo_C[b] = xo_all + (int64_t)b * nr;
     M.write_PRC_C[b] = (micsa_prc_t *)xmalloc(sizeof(micsa_prc_t) * nr);
     M.write_xo_C[b] = (micsa_xoshiro_t *)xmalloc(sizeof(micsa_xoshiro_t) * nr);
     for (int r = 0; r < nr; r++) {
@@ -626,27 +631,32 @@ static void *refresh_worker(void *arg) {
   return NULL;
 }
 
-/* refresh_walkers (main.cu:340-377) with the draws on the GPU: the walkers
- * the reference would upload now are the next draws of each stream, so they
- * are drawn now, on the device, from the streams' current state; the
- * snapshot written with the next checkpoint is the state after them, as in
- * the reference.  A resumed run first uploads the walkers of its checkpoint. */
+/* refresh_walkers (main.cu:340-377) with the draws on the GPU.  As in the
+ * reference, the next walkers are drawn while the GPU runs: there a host
+ * thread, here a draw on a side stream (micsa_refresh_demons_ahead).  At a
+ * refresh the walkers drawn ahead become current, the snapshot written with
+ * the next checkpoint is the streams' state after them, and the next draw
+ * starts.  A resumed run first uploads the walkers of its checkpoint. */
 static void refresh_walkers_gpu(micsa_ctx *ctx, int *first) {
-  for (int b = 0; b < M.nbits; b++) {
-    if (!(*first * data.flag)) {
-      int rc;
-      if (*first) {
-        rc = micsa_upload_demons(ctx, b, M.w0[b], M.w1[b]);
-      } else {
-        rc = micsa_refresh_demons(ctx, b, 1, M.random_PRC_C[b], M.random_xo_C[b], M.thr);
-      }
-      if (rc) die("demon refresh: %s\n", micsa_last_error(ctx));
+  int rc = 0;
+  if (!(*first && data.flag)) {
+    if (*first) {
+      for (int b = 0; b < M.nbits && !rc; b++) rc = micsa_upload_demons(ctx, b, M.w0[b], M.w1[b]);
+    } else {
+      rc = micsa_refresh_commit(ctx);
+    }
+    if (!rc) rc = micsa_refresh_wait(ctx);
+    if (rc) die("demon refresh: %s\n", micsa_last_error(ctx));
+    for (int b = 0; b < M.nbits; b++) {
       memcpy(M.write_PRC_C[b], M.random_PRC_C[b], sizeof(micsa_prc_t) * M.nr);
       memcpy(M.write_xo_C[b], M.random_xo_C[b], sizeof(micsa_xoshiro_t) * M.nr);
     }
-    M.icds[b].first = 0; /* InitWalkers, ini.c:739-741 */
   }
+  for (int b = 0; b < M.nbits; b++) M.icds[b].first = 0; /* InitWalkers, ini.c:739-741 */
   *first = 0;
+  /* the next walkers, from the streams as they stand (InitWalkers thread) */
+  if ((rc = micsa_refresh_demons_ahead(ctx, 0, M.nbits, M.random_PRC_C[0], M.random_xo_C[0], M.thr)))
+    die("demon refresh: %s\n", micsa_last_error(ctx));
 }
 
 /* refresh_walkers (main.cu:340-377) */

@@ -164,7 +164,16 @@ static void *run_group(void *arg) {
       /* the host advance of the streams overlaps the iterations that follow */
       if (!(t & (t - 1))) {
         if (!has_schedule(j0)) {
-          CK(micsa_refresh_demons_async(ctx, 0, nrun, prc, xo, thr));
+          /* refresh t was drawn ahead (except at t = 0); draw the next one,
+           * for the jobs that run past it, while these iterations run */
+          if (t == 0)
+            CK(micsa_refresh_demons_async(ctx, 0, nrun, prc, xo, thr));
+          else
+            CK(micsa_refresh_commit(ctx));
+          const int64_t tn = t ? 2 * t : 1;
+          int nnext = 0;
+          while (nnext < nrun && gr->jobs[gr->idx[nnext]].iterations > tn) nnext++;
+          if (nnext) CK(micsa_refresh_demons_ahead(ctx, 0, nnext, prc, xo, thr));
         } else { /* each job at its own point of its beta schedule */
           for (int k = 0; k < nrun; k++) {
             uint64_t tk[3];

@@ -21,6 +21,7 @@ ABI_SYMBOLS = [
     "micsa_create", "micsa_destroy", "micsa_last_error", "micsa_footprint_bytes",
     "micsa_set_lut", "micsa_upload_couplings", "micsa_upload_spins", "micsa_upload_demons",
     "micsa_refresh_demons", "micsa_refresh_demons_async", "micsa_refresh_wait",
+    "micsa_refresh_demons_ahead", "micsa_refresh_commit",
     "micsa_monte_carlo", "micsa_iterate", "micsa_measure", "micsa_download_spins",
     "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_energy_noalloc",
     "micsa_synchronize", "micsa_kernel_launches", "micsa_stream", "micsa_job_measurements",
@@ -116,6 +117,9 @@ def lib():
         "micsa_refresh_demons_async": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(PRC),
                                                  C.POINTER(Xoshiro), u64p]),
         "micsa_refresh_wait": (C.c_int, [C.c_void_p]),
+        "micsa_refresh_demons_ahead": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(PRC),
+                                                 C.POINTER(Xoshiro), u64p]),
+        "micsa_refresh_commit": (C.c_int, [C.c_void_p]),
         "micsa_monte_carlo": (C.c_int, [C.c_void_p, C.c_int, u32p, u32p]),
         "micsa_iterate": (C.c_int, [C.c_void_p, C.c_int64]),
         "micsa_measure": (C.c_int, [C.c_void_p, i32p, u64p, i64p, i64p]),
@@ -263,6 +267,20 @@ class Context:
         """Per-sample run flags (None: all samples run)."""
         a = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8)
         check(self.h, lib().micsa_set_active(self.h, _ptr(a, C.c_uint8)), "set_active")
+
+    def refresh_demons_ahead(self, first, prc, xo, thr):
+        """Draw the next refresh into the back buffer on the side stream
+        (prc/xo advanced in the background, as refresh_demons_async)."""
+        count, rem = divmod(len(prc), self.nr)
+        if rem or len(xo) != len(prc):
+            raise ValueError("need count*nr streams of each generator")
+        self._thr_a = np.ascontiguousarray(thr, dtype=np.uint64)
+        check(self.h, lib().micsa_refresh_demons_ahead(self.h, first, count, prc, xo,
+                                                       _ptr(self._thr_a, C.c_uint64)),
+              "refresh_demons_ahead")
+
+    def refresh_commit(self):
+        check(self.h, lib().micsa_refresh_commit(self.h), "refresh_commit")
 
     def refresh_wait(self):
         check(self.h, lib().micsa_refresh_wait(self.h), "refresh_wait")

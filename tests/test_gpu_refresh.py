@@ -147,3 +147,45 @@ def test_gpu_refresh_async_overlaps_and_matches():
     assert bytes(prc) == bytes(hp) and bytes(xo) == bytes(hx)
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_gpu_refresh_ahead_equals_in_place():
+    """Refreshes drawn ahead on the side stream while iterations run, then
+    committed, give the demons, spins and stream structs of in-place
+    refreshes at the same points; committing with nothing pending fails."""
+    L, nr, nc, ns = 16, 64, 3, 2
+    thr = micsa.thresholds(BETA)
+    H, V = (L // 4) ** 3 // 2, L ** 3
+    prc, xo = _streams(ns * nr, 4242)
+    hp, hx = _copy(prc, micsa.PRC), _copy(xo, micsa.Xoshiro)
+    out = []
+    for ahead, (p_, x_) in ((True, (prc, xo)), (False, (hp, hx))):
+        r2 = np.random.default_rng(9)
+        with micsa.Context(L, nr, ns, nc) as ctx:
+            for s in range(ns):
+                J = micsa.pack_couplings(L, *(r2.integers(0, 2, size=V, dtype=np.uint8) for _ in range(3)))
+                ctx.upload_couplings(s, J)
+                ctx.upload_spins(s, *(r2.integers(0, 2 ** 64 - 1, size=H * nr, dtype=np.uint64,
+                                                  endpoint=True) for _ in range(2)))
+            if ahead:
+                with pytest.raises(micsa.MicsaError, match="ERR_STATE"):
+                    ctx.refresh_commit()
+                ctx.refresh_demons(0, p_, x_, thr)
+                ctx.refresh_demons_ahead(0, p_, x_, thr)
+                for _ in range(3):
+                    ctx.iterate(2)
+                    ctx.refresh_commit()
+                    ctx.refresh_demons_ahead(0, p_, x_, thr)
+                ctx.iterate(2)
+            else:
+                ctx.refresh_demons(0, p_, x_, thr)
+                for _ in range(3):
+                    ctx.iterate(2)
+                    ctx.refresh_demons(0, p_, x_, thr)
+                ctx.iterate(2)
+                ctx.refresh_demons(0, p_, x_, thr)  # the draw the other run left pending
+            ctx.refresh_wait()
+            out.append([ctx.download_spins(s) for s in range(ns)] + [ctx.measure()["e_demon"]])
+    assert bytes(prc) == bytes(hp) and bytes(xo) == bytes(hx)
+    for a, b in zip(out[0][:ns], out[1][:ns]):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
