@@ -50,7 +50,7 @@ def test_gpu_reproduces_reference(golden):
 @pytest.mark.parametrize("L,nr,nc,ns,iters", [
     (8, 32, 6, 1, 9), (8, 64, 2, 3, 5), (16, 32, 6, 2, 17), (16, 96, 3, 1, 4),
     (24, 32, 6, 1, 13), (32, 64, 6, 2, 3), (40, 32, 4, 1, 21), (48, 128, 6, 1, 2),
-    (64, 64, 6, 1, 2),
+    (64, 64, 6, 1, 2), (64, 64, 6, 8, 3), (96, 32, 6, 2, 2), (56, 64, 5, 3, 4),
 ])
 def test_gpu_matches_oracle_random_state(L, nr, nc, ns, iters):
     """Arbitrary states (not reachable from seeds), many iterations so the
