@@ -640,6 +640,34 @@ k_demon_energy(const micsa_geo g, const uint32_t *__restrict__ d0, const uint32_
   atomicAdd(dem + (int64_t)s * g.nr + w * 32 + lane, acc);
 }
 
+/* Demon energy with 16-byte loads, for W in {1, 2, 4}: a plane (sample s,
+ * plane pi) is P*W consecutive words; component c of a lane's 4-word vector
+ * at word 4k is word w = c % W of its site (4 % W == 0), the same for every
+ * lane, so one transpose per component gives lane l the count of replica
+ * w*32 + l.  blockIdx.y = s*2*nc + pi; blocks stride over the plane. */
+__global__ void __launch_bounds__(TPB)
+k_demon_energy_v4(const micsa_geo g, const uint32_t *__restrict__ d0,
+                  const uint32_t *__restrict__ d1, unsigned long long *__restrict__ dem) {
+  const int plane = blockIdx.y, s = plane / (2 * g.nc), lane = threadIdx.x & 31;
+  if (micsa_frozen(g, s)) return;
+  const int64_t nvec = g.P * g.W / 4; /* P is a multiple of 32 */
+  const uint4 *a = (const uint4 *)(d0 + (int64_t)plane * g.P * g.W);
+  const uint4 *b = (const uint4 *)(d1 + (int64_t)plane * g.P * g.W);
+  unsigned long long acc[4] = {0, 0, 0, 0};
+  const int64_t step = (int64_t)gridDim.x * TPB;
+  for (int64_t base = (int64_t)blockIdx.x * TPB + (threadIdx.x & ~31); base < nvec; base += step) {
+    const int64_t i = base + lane; /* nvec is a multiple of 32: whole warps */
+    const uint4 x = __ldcs(a + i), y = __ldcs(b + i);
+    acc[0] += __popc(warp_transpose32(x.x, lane)) + 2u * __popc(warp_transpose32(y.x, lane));
+    acc[1] += __popc(warp_transpose32(x.y, lane)) + 2u * __popc(warp_transpose32(y.y, lane));
+    acc[2] += __popc(warp_transpose32(x.z, lane)) + 2u * __popc(warp_transpose32(y.z, lane));
+    acc[3] += __popc(warp_transpose32(x.w, lane)) + 2u * __popc(warp_transpose32(y.w, lane));
+  }
+  for (int c = g.W; c < 4; c++) acc[c % g.W] += acc[c]; /* component c is word c % W */
+  unsigned long long *out = dem + (int64_t)s * g.nr + lane;
+  for (int w = 0; w < g.W; w++) atomicAdd(out + w * 32, acc[w]);
+}
+
 /* Overlap and C4 of the replica pairs (2k, 2k+1): with t = s(x) ^ s(x'),
  * bit 2k of t ^ (t >> 1) is d_x xor d_x', d = a xor b the pair difference.
  * blockIdx.y = axis*nd + dist (dist 0 also yields q via x' = x and the
@@ -782,6 +810,13 @@ cudaError_t micsa_launch_energy(const micsa_geo &g, const uint32_t *spin, const 
 
 cudaError_t micsa_launch_demon_energy(const micsa_geo &g, const uint32_t *d0, const uint32_t *d1,
                                       unsigned long long *dem, cudaStream_t st) {
+  if (g.W == 1 || g.W == 2 || g.W == 4) {
+    const int64_t planes = (int64_t)2 * g.nc * g.ns, vec_blocks = (g.P * g.W / 4 + TPB - 1) / TPB;
+    int64_t bx = (8 * 152 + planes - 1) / planes; /* about 8 blocks per SM in all */
+    if (bx > vec_blocks) bx = vec_blocks;
+    k_demon_energy_v4<<<dim3((unsigned)(bx < 1 ? 1 : bx), (unsigned)planes), TPB, 0, st>>>(g, d0, d1, dem);
+    return cudaGetLastError();
+  }
   dim3 grid(measure_blocks(g.P, (int64_t)2 * g.nc * g.W * g.ns), 2 * g.nc * g.W, g.ns);
   k_demon_energy<<<grid, TPB, 0, st>>>(g, d0, d1, dem);
   return cudaGetLastError();
