@@ -20,7 +20,7 @@
 #include "micsa_jump.h"
 #include "micsa_kernels.cuh"
 
-#define MICSA_TUNE_MAX 64
+#define MICSA_TUNE_MAX 96
 
 struct micsa_ctx {
   micsa_config cfg;
@@ -42,10 +42,12 @@ struct micsa_ctx {
   int64_t launches = 0;
   int resident = 0;        /* small lattice: iterations run in shared memory */
   int split = 0;           /* 1: one half-sweep launch per sample (smaller L2 working set) */
+  micsa_tma tma = {};      /* tensor maps of the demon arrays (staged sweep) */
   int64_t graph_launches = 0; /* kernels per replay of the iteration graph */
   int ntune = 0;           /* launch shapes timed at creation */
   int tune_zc[MICSA_TUNE_MAX] = {0}, tune_pd[MICSA_TUNE_MAX] = {0};
   int tune_split[MICSA_TUNE_MAX] = {0}, tune_occ[MICSA_TUNE_MAX] = {0};
+  int tune_tma[MICSA_TUNE_MAX] = {0};
   double tune_ms[MICSA_TUNE_MAX] = {0};
   /* demon refresh on the device: jump tables of one segment length */
   micsa_refresh_plan plan = {};
@@ -192,15 +194,17 @@ cudaError_t launch_half(micsa_ctx *ctx, const micsa_geo &g, int s, int p, int ic
   if (launches) ++*launches;
   if (s < 0)
     return micsa_launch_sweep_micsa(g, p, ic, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb, ctx->walk,
-                                    ctx->stream);
+                                    &ctx->tma, ctx->stream);
   const size_t PW = (size_t)g.P * g.W;
   micsa_geo g1 = g;
   g1.ns = 1;
+  g1.s0 = s; /* the staged sweep addresses the whole demon arrays */
   g1.active = g.active ? g.active + s : nullptr; /* a frozen sample returns at once */
   return micsa_launch_sweep_micsa(g1, p, ic, ctx->spin + s * 2 * PW,
                                   ctx->dem0 + s * 2 * (size_t)g.nc * PW,
                                   ctx->dem1 + s * 2 * (size_t)g.nc * PW,
-                                  ctx->jb + (size_t)s * 2 * g.P, ctx->walk + s, ctx->stream);
+                                  ctx->jb + (size_t)s * 2 * g.P, ctx->walk + s, &ctx->tma,
+                                  ctx->stream);
 }
 
 /* The half-sweeps of one iteration (ic = ic0 .. ic1-1).  split = 0: plane by
@@ -247,9 +251,11 @@ int autotune(micsa_ctx *ctx) {
                   zc, pd, g.L);
     g.zc = zc;
     g.pd = pd;
-    const char *es = getenv("MICSA_SWEEP_SPLIT"), *eo = getenv("MICSA_SWEEP_OCC");
+    const char *es = getenv("MICSA_SWEEP_SPLIT"), *eo = getenv("MICSA_SWEEP_OCC"),
+               *et = getenv("MICSA_SWEEP_TMA");
     ctx->split = es && atoi(es) && g.ns > 1;
     g.occ = eo && atoi(eo) == 4 ? 4 : 3;
+    g.tma = et && atoi(et) && ctx->tma.ok;
     ctx->ntune = 0;
     return MICSA_OK;
   }
@@ -257,17 +263,20 @@ int autotune(micsa_ctx *ctx) {
   MICSA_CK(cudaEventCreate(&e0));
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
-  int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, n = 0;
+  int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, best_tma = 0, n = 0;
   const int reps = 2;
   const int nocc = g.W % 4 ? 2 : 1; /* the 4-blocks variant exists for VW <= 2 */
+  for (int tm = 0; tm < (ctx->tma.ok ? 2 : 1); tm++)
   for (int oc = 0; oc < nocc; oc++)
   for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
   for (int c = 0; c < nz; c++)
     for (int d = 0; d < 3; d++) {
       if (pds[d] && pds[d] >= zcs[c]) continue; /* prefetch only within a slab */
+      if (tm && zcs[c] > 4) continue;              /* staged tiles: at most 4 planes */
       g.zc = zcs[c];
       g.pd = pds[d];
       g.occ = oc ? 4 : 3;
+      g.tma = tm;
       for (int rep = -1; rep < reps; rep++) { /* rep -1: warm-up */
         if (rep == 0) MICSA_CK(cudaEventRecord(e0, ctx->stream));
         MICSA_CK(launch_halves(ctx, g, sp, 0, g.nc, nullptr)); /* one iteration's order */
@@ -282,6 +291,7 @@ int autotune(micsa_ctx *ctx) {
         ctx->tune_pd[n] = g.pd;
         ctx->tune_split[n] = sp;
         ctx->tune_occ[n] = g.occ;
+        ctx->tune_tma[n] = g.tma;
         ctx->tune_ms[n] = per;
         n++;
       }
@@ -291,6 +301,7 @@ int autotune(micsa_ctx *ctx) {
         best_pd = g.pd;
         best_split = sp;
         best_occ = g.occ;
+        best_tma = g.tma;
       }
     }
   ctx->ntune = n;
@@ -298,6 +309,7 @@ int autotune(micsa_ctx *ctx) {
   g.pd = best_pd;
   ctx->split = best_split;
   g.occ = best_occ;
+  g.tma = best_tma;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return MICSA_OK;
@@ -348,6 +360,8 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.zc = 0;
   g.pd = 0;
   g.occ = 3;
+  g.tma = 0;
+  g.s0 = 0;
   g.H = s.H;
   g.active = nullptr;
   ctx->stage_words = (size_t)s.stage_w;
@@ -401,6 +415,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
                                            cfg->device));
     ctx->resident = need > 0 && need <= (size_t)optin && !(er && !strcmp(er, "0"));
   }
+  MICSA_CK_CREATE(micsa_make_tma(ctx->g, ctx->dem0, ctx->dem1, &ctx->tma));
   if ((rc = autotune(ctx)) != MICSA_OK) {
     fprintf(stderr, "micsa_create: autotune: %s\n", ctx->err);
     micsa_destroy(ctx);
@@ -417,11 +432,12 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d |", ctx->g.zc, ctx->g.pd, ctx->split,
-                   ctx->g.occ);
+  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d tma=%d |", ctx->g.zc, ctx->g.pd,
+                   ctx->split, ctx->g.occ, ctx->g.tma);
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
-    k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d:%.5fms", ctx->tune_zc[c], ctx->tune_pd[c],
-                  ctx->tune_split[c], ctx->tune_occ[c], ctx->tune_ms[c]);
+    k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],
+                  ctx->tune_pd[c], ctx->tune_split[c], ctx->tune_occ[c], ctx->tune_tma[c],
+                  ctx->tune_ms[c]);
   return MICSA_OK;
 }
 
@@ -963,6 +979,9 @@ int micsa_synchronize(micsa_ctx *ctx) {
   if (rc) return rc;
   MICSA_CK(cudaStreamSynchronize(ctx->stream));
   MICSA_CK(cudaGetLastError());
+  unsigned to = 0;
+  MICSA_CK(micsa_tma_timeout_count(&to));
+  if (to) return fail(ctx, MICSA_ERR_CUDA, "%u staged demon loads timed out (read directly)", to);
   return MICSA_OK;
 }
 

@@ -8,6 +8,10 @@
  * half-sweep streams one demon plane (read + write) and the spins of both
  * colours; there is no contraction for tensor cores.
  */
+#include <string.h>
+
+#include <cuda.h> /* CUtensorMap and the encode function's types (resolved at run time) */
+
 #include "micsa_kernels.cuh"
 
 namespace {
@@ -173,6 +177,44 @@ __device__ __forceinline__ uint32_t metropolis_flip(uint32_t j1, uint32_t j2, ui
 }
 
 /* Loads of 2*VW consecutive words (the same VW words of two adjacent sites). */
+/* ----------------------------------------------- TMA and mbarriers */
+/* transaction barriers in shared memory, bulk tensor loads (sm_90+ PTX) */
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+/* bounded wait on phase `phase`; false if the limit ran out */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase) {
+  const uint32_t a = smem_addr(bar);
+  for (int i = 0; i < (1 << 20); i++) {
+    uint32_t done;
+    asm volatile("{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2; selp.u32 %0, 1, 0, q; }"
+                 : "=r"(done) : "r"(a), "r"(phase) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+/* box of the 3-d tensor `map` at (x, y, z) into shared memory; completes on bar */
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *map, int x, int y, int z,
+                                            uint64_t *bar) {
+  asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+               " [%0], [%1, {%2, %3, %4}], [%5];"
+               ::"r"(smem_addr(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+               : "memory");
+}
+/* waits that ran out (a TMA copy that never completed): counted, and the
+ * sweep falls back to global loads for that step */
+__device__ unsigned int micsa_tma_timeouts;
+
 template <int VW> struct pair_io;
 template <> struct pair_io<1> {
   static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[2], uint64_t p) { hint<2>::ld_nc(a, o, p); }
@@ -261,12 +303,13 @@ template <int VW, bool WIDE> struct pairs {
  * bytes and the two demon words per plane.  Block = (TX pairs along x/2) x
  * (TY rows); TX divides L/4; grid = (L/4/TX, ytiles*ns*G, L/zc).
  * In-plane offsets are 32-bit (P*W < 2^32 is checked at creation). */
-template <int VW, bool MICSA, bool WIDE, int MINB>
+template <int VW, bool MICSA, bool WIDE, int MINB, bool TMA>
 __global__ void __launch_bounds__(TPB, MINB)
 k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
         const int zc, const int pd, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
         uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
-        const int *__restrict__ walk, const uint32_t *__restrict__ rnd) {
+        const int *__restrict__ walk, const uint32_t *__restrict__ rnd,
+        const __grid_constant__ micsa_tma tm) {
   constexpr int N = 2 * VW; /* words per pair */
   using PR = pairs<VW, WIDE>;
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
@@ -322,6 +365,51 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
     q1b = d1 + base;
   }
 
+  /* TMA variant (W == VW, whole row tiles): the block's demon tile in each
+   * of its zc planes -- blockDim.y rows of the block's 2*blockDim.x pairs,
+   * shifted by the walk -- is loaded by one thread into shared memory at the
+   * start, completing on one mbarrier per plane.  The box is 4 words wider
+   * than the tile so that its start can be rounded down to 16 bytes; tiles
+   * that would wrap around the lattice keep the global loads. */
+  extern __shared__ __align__(128) uint32_t smem_dyn[];
+  uint64_t *bars = nullptr;
+  int off = 0;
+  bool staged = false;
+  if (TMA && MICSA) {
+    const int k = __ldg(walk + s);
+    const int sh = ((p == 0) == (ic < 3)) ? k : -k;
+    const int axis = ic < 3 ? ic : ic - 3;
+    const int xb = 2 * blockIdx.x * blockDim.x, yb = tile * blockDim.y;
+    int cx = xb, ry = yb;
+    if (axis == 0) { cx = xb - sh; cx += cx < 0 ? (int)Lh : (cx >= (int)Lh ? -(int)Lh : 0); }
+    if (axis == 1) { ry = yb - 2 * sh; ry += ry < 0 ? (int)L : (ry >= (int)L ? -(int)L : 0); }
+    const int c0 = cx * VW, cal = c0 & ~3;
+    off = c0 - cal;
+    staged = cx + 2 * (int)blockDim.x <= (int)Lh && ry + (int)blockDim.y <= (int)L &&
+             off + 2 * (int)blockDim.x * VW <= tm.box_w;
+    const int tile_words = (int)blockDim.y * tm.box_w;
+    bars = (uint64_t *)(smem_dyn + 2 * zc * tile_words);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (staged) {
+      if (tid == 0) {
+        for (int t = 0; t < zc; t++) mbar_init(bars + t, 1);
+        mbar_fence_init();
+      }
+      __syncthreads();
+      if (tid == 0) {
+        const int zplane = (((g.s0 + (int)s) * 2 + p) * g.nc + ic) * (int)L;
+        for (int t = 0; t < zc; t++) {
+          int zt = (int)zd + t;
+          zt -= zt >= (int)L ? (int)L : 0;
+          mbar_expect_tx(bars + t, 2u * (uint32_t)tile_words * 4u);
+          tma_load_3d(smem_dyn + (2 * t) * tile_words, &tm.map[0], cal, ry, zplane + zt, bars + t);
+          tma_load_3d(smem_dyn + (2 * t + 1) * tile_words, &tm.map[1], cal, ry, zplane + zt,
+                      bars + t);
+        }
+      }
+    }
+  }
+
   /* other colour at (2j, 2j+1; y) for planes z0-1 and z0 */
   uint32_t vm[N], v0[N];
   PR::ld_nc(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, W, vm, keep);
@@ -340,25 +428,44 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
     PR::ld_nc(oth + (zo + rowS) * W, W, vs, keep);
     hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
     const uint32_t jb2 = ld_u16_keep(jbp + zo + row, keep);
-    if (MICSA) {
-      const uint32_t sa = (zdd * plane + drowA) * W;
-      if (dpair) {
-        PR::ld_na(q0b + sa, W, a0, strm);
-        PR::ld_na(q1b + sa, W, a1, strm);
-      } else {
-        const uint32_t sb = (zdd * plane + drowB) * W;
-        uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
-        hint<VW>::ld_na(q0b + sa, x0, strm);
-        hint<VW>::ld_na(q0b + sb, x1, strm);
-        hint<VW>::ld_na(q1b + sa, y0, strm);
-        hint<VW>::ld_na(q1b + sb, y1, strm);
+    bool from_smem = false;
+    if (TMA && staged) {
+      if (mbar_wait(bars + t, 0)) {
+        const int tile_words = (int)blockDim.y * tm.box_w;
+        const uint32_t *r0 = smem_dyn + (2 * t) * tile_words + threadIdx.y * tm.box_w + off +
+                             2 * threadIdx.x * VW;
+        const uint32_t *r1 = r0 + tile_words;
 #pragma unroll
-        for (int w = 0; w < VW; w++) {
-          a0[w] = x0[w]; a0[VW + w] = x1[w];
-          a1[w] = y0[w]; a1[VW + w] = y1[w];
+        for (int w = 0; w < N; w++) {
+          a0[w] = r0[w];
+          a1[w] = r1[w];
+        }
+        from_smem = true;
+      } else {
+        atomicAdd(&micsa_tma_timeouts, 1u);
+      }
+    }
+    if (MICSA) {
+      if (!from_smem) {
+        const uint32_t sa = (zdd * plane + drowA) * W;
+        if (dpair) {
+          PR::ld_na(q0b + sa, W, a0, strm);
+          PR::ld_na(q1b + sa, W, a1, strm);
+        } else {
+          const uint32_t sb = (zdd * plane + drowB) * W;
+          uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
+          hint<VW>::ld_na(q0b + sa, x0, strm);
+          hint<VW>::ld_na(q0b + sb, x1, strm);
+          hint<VW>::ld_na(q1b + sa, y0, strm);
+          hint<VW>::ld_na(q1b + sb, y1, strm);
+#pragma unroll
+          for (int w = 0; w < VW; w++) {
+            a0[w] = x0[w]; a0[VW + w] = x1[w];
+            a1[w] = y0[w]; a1[VW + w] = y1[w];
+          }
         }
       }
-      if (pd > 0 && t + (uint32_t)pd < (uint32_t)zc) {
+      if (!staged && pd > 0 && t + (uint32_t)pd < (uint32_t)zc) {
         uint32_t zf = zdd + (uint32_t)pd;
         if (zf >= L) zf -= L;
         prefetch_l2(q0b + (zf * plane + drowA) * W);
@@ -718,16 +825,22 @@ inline int blocks_for(int64_t n, int per_block) {
 
 /* ------------------------------------------------------------ launchers */
 
+/* tile of the sweep for this L: tx pairs along x/2 (the largest power of two
+ * <= 32 dividing L/4, L/4 even) x ty rows, ty*tx = TPB threads */
+static void sweep_tile(int L, int *tx, int *ty) {
+  int x = 32;
+  while ((L / 4) % x) x >>= 1;
+  *tx = x;
+  *ty = TPB / x;
+}
+
 template <int VW>
 static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint32_t *spin,
                             uint32_t *d0, uint32_t *d1, const uint8_t *jb, const int *walk,
-                            const uint32_t *rnd, cudaStream_t st) {
+                            const uint32_t *rnd, const micsa_tma *tm, cudaStream_t st) {
   const int G = g.W / VW;
-  /* TX site pairs along x/2 per block row: the largest power of two <= 32
-   * that divides L/4 (L/4 is even) */
-  int tx = 32;
-  while ((g.Lh / 2) % tx) tx >>= 1;
-  const int ty = TPB / tx;
+  int tx, ty;
+  sweep_tile(g.L, &tx, &ty);
   const int ytiles = (g.L + ty - 1) / ty;
   /* z chunk per thread: long columns at large L, more threads at small L */
   const int zc = g.zc > 0 ? g.zc : ((g.L >= 128 && g.L % 16 == 0) ? 16 : (g.L >= 48 ? 8 : 2));
@@ -736,37 +849,99 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
   /* blocks per SM the register allocation is made for: the default (3, or
    * 2 for 4-word vectors), or occ = 4 (at most 64 registers, VW <= 2) */
   constexpr int B0 = VW == 4 ? 2 : 3, B1 = VW == 4 ? 2 : 4;
-#define MICSA_SWEEP(M, WD, B) \
-  k_sweep<VW, M, WD, B><<<grid, block, 0, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd)
+  /* TMA-staged demon tiles: one word group per site, whole row tiles, at
+   * most 4 planes per block (shared memory 2*zc tiles + zc barriers) */
+  const bool tma = micsa && tm && tm->ok && g.tma && G == 1 && g.L % ty == 0 && zc <= 4 &&
+                   tm->ty == ty && tm->box_w >= 2 * tx * VW;
+  const size_t smem = tma ? (size_t)2 * zc * ty * tm->box_w * 4 + (size_t)zc * 8 : 0;
+  micsa_tma none;
+  const micsa_tma &t = tm ? *tm : none;
+#define MICSA_SWEEP(M, WD, B, T)                                                                  \
+  do {                                                                                            \
+    if (T && smem > 48 * 1024) {                                                                  \
+      const cudaError_t e_ = cudaFuncSetAttribute(k_sweep<VW, M, WD, B, T>,                       \
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                                                  (int)smem);                                     \
+      if (e_ != cudaSuccess) return e_;                                                           \
+    }                                                                                             \
+    k_sweep<VW, M, WD, B, T><<<grid, block, smem, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0,  \
+                                                        d1, jb, walk, rnd, t);                   \
+  } while (0)
   if (G == 1) {
-    if (micsa) { if (g.occ == 4) MICSA_SWEEP(true, true, B1); else MICSA_SWEEP(true, true, B0); }
-    else MICSA_SWEEP(false, true, B0);
+    if (micsa) {
+      if (tma) { if (g.occ == 4) MICSA_SWEEP(true, true, B1, true); else MICSA_SWEEP(true, true, B0, true); }
+      else { if (g.occ == 4) MICSA_SWEEP(true, true, B1, false); else MICSA_SWEEP(true, true, B0, false); }
+    } else {
+      MICSA_SWEEP(false, true, B0, false);
+    }
   } else {
-    if (micsa) { if (g.occ == 4) MICSA_SWEEP(true, false, B1); else MICSA_SWEEP(true, false, B0); }
-    else MICSA_SWEEP(false, false, B0);
+    if (micsa) { if (g.occ == 4) MICSA_SWEEP(true, false, B1, false); else MICSA_SWEEP(true, false, B0, false); }
+    else MICSA_SWEEP(false, false, B0, false);
   }
 #undef MICSA_SWEEP
   return cudaGetLastError();
 }
 
+cudaError_t micsa_make_tma(const micsa_geo &g, const uint32_t *d0, const uint32_t *d1,
+                           micsa_tma *out) {
+  memset(out, 0, sizeof *out);
+  if (g.W != 1 && g.W != 2 && g.W != 4) return cudaSuccess;
+  typedef CUresult (*encode_t)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                               const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                               const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                               CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                   cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+    cudaGetLastError();
+    return cudaSuccess; /* no staged sweep; not an error */
+  }
+  int tx, ty;
+  sweep_tile(g.L, &tx, &ty);
+  const cuuint64_t row = (cuuint64_t)g.Lh * g.W; /* words per (plane, y) row */
+  /* the tile plus 4 words (16 bytes) for a start rounded down, at most a row */
+  int box_w = 2 * tx * g.W + 4;
+  if (box_w > (int)row) box_w = (int)row;
+  if (box_w > 256 || ty > 256 || box_w % 4 || ty > g.L) return cudaSuccess;
+  const cuuint64_t dims[3] = {row, (cuuint64_t)g.L, (cuuint64_t)g.L * g.ns * 2 * g.nc};
+  const cuuint64_t strides[2] = {row * 4, row * 4 * (cuuint64_t)g.L};
+  const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)ty, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const uint32_t *base[2] = {d0, d1};
+  for (int k = 0; k < 2; k++) {
+    const CUresult r = ((encode_t)fn)((CUtensorMap *)out->map[k], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3,
+                                      (void *)base[k], dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaSuccess;
+  }
+  out->box_w = box_w;
+  out->ty = ty;
+  out->ok = 1;
+  return cudaSuccess;
+}
+
 static cudaError_t sweep_any(const micsa_geo &g, int p, int ic, bool micsa, uint32_t *spin,
                              uint32_t *d0, uint32_t *d1, const uint8_t *jb, const int *walk,
-                             const uint32_t *rnd, cudaStream_t st) {
-  if (g.W % 4 == 0) return sweep_vw<4>(g, p, ic, micsa, spin, d0, d1, jb, walk, rnd, st);
-  if (g.W % 2 == 0) return sweep_vw<2>(g, p, ic, micsa, spin, d0, d1, jb, walk, rnd, st);
-  return sweep_vw<1>(g, p, ic, micsa, spin, d0, d1, jb, walk, rnd, st);
+                             const uint32_t *rnd, const micsa_tma *tm, cudaStream_t st) {
+  if (g.W % 4 == 0) return sweep_vw<4>(g, p, ic, micsa, spin, d0, d1, jb, walk, rnd, tm, st);
+  if (g.W % 2 == 0) return sweep_vw<2>(g, p, ic, micsa, spin, d0, d1, jb, walk, rnd, tm, st);
+  return sweep_vw<1>(g, p, ic, micsa, spin, d0, d1, jb, walk, rnd, tm, st);
 }
 
 cudaError_t micsa_launch_sweep_micsa(const micsa_geo &g, int p, int ic, uint32_t *spin,
                                      uint32_t *d0, uint32_t *d1, const uint8_t *jb,
-                                     const int *walk, cudaStream_t st) {
-  return sweep_any(g, p, ic, true, spin, d0, d1, jb, walk, nullptr, st);
+                                     const int *walk, const micsa_tma *tm, cudaStream_t st) {
+  return sweep_any(g, p, ic, true, spin, d0, d1, jb, walk, nullptr, tm, st);
 }
 
 cudaError_t micsa_launch_sweep_metropolis(const micsa_geo &g, int p, uint32_t *spin,
                                           const uint8_t *jb, const uint32_t *rnd,
                                           cudaStream_t st) {
-  return sweep_any(g, p, 0, false, spin, nullptr, nullptr, jb, nullptr, rnd, st);
+  return sweep_any(g, p, 0, false, spin, nullptr, nullptr, jb, nullptr, rnd, nullptr, st);
 }
 
 cudaError_t micsa_launch_gen_rnd(const micsa_geo &g, int p, const uint32_t *te,
@@ -1081,4 +1256,8 @@ cudaError_t micsa_launch_resident(const micsa_geo &g, int n, uint32_t *spin, uin
   if (g.L == 8) return resident_l<8>(g, n, spin, d0, d1, jb, walk, st);
   if (g.L == 16) return resident_l<16>(g, n, spin, d0, d1, jb, walk, st);
   return cudaErrorInvalidValue;
+}
+
+cudaError_t micsa_tma_timeout_count(unsigned *n) {
+  return cudaMemcpyFromSymbol(n, micsa_tma_timeouts, sizeof(unsigned));
 }

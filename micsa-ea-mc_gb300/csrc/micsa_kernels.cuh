@@ -29,6 +29,8 @@ struct micsa_geo {
   int zc;     /* z planes per thread in the sweeps (divides L; 0 = default) */
   int pd;     /* L2 prefetch distance of the demon stream, in z steps (0 = off) */
   int occ;    /* sweep variant: 4 = register cap for 4 blocks per SM, else the compiler's */
+  int tma;    /* 1: the sweep stages its demon tiles in shared memory by TMA */
+  int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */
 };
@@ -37,14 +39,33 @@ __host__ __device__ inline bool micsa_frozen(const micsa_geo &g, int s) {
   return g.active && !g.active[s];
 }
 
+/* Tensor maps of the two demon arrays for the TMA-staged sweep: each array
+ * seen as [planes (s, p, ic, z)][y][x/2 * W] 32-bit words; box = the demon
+ * tile of one block in one z plane (box_w words x ty rows).  Opaque storage
+ * for two CUtensorMap objects. */
+struct micsa_tma {
+  alignas(64) unsigned char map[2][128];
+  int box_w, ty;
+  int ok; /* built */
+};
+/* Build the maps for the context's demon arrays (0 when this L, W or the
+ * driver does not allow the staged sweep: then ok = 0). */
+cudaError_t micsa_make_tma(const micsa_geo &g, const uint32_t *d0, const uint32_t *d1,
+                           micsa_tma *out);
+
+/* waits of the staged sweep that ran out since the process started (0 unless
+ * a TMA copy never completed; the sweep then read the words directly) */
+cudaError_t micsa_tma_timeout_count(unsigned *n);
+
 /* slab depths the sweep can use for this L (divisors of L, ascending) */
 int micsa_sweep_zc_candidates(int L, int *out, int max);
 
-/* flag = 1 half-sweep of colour p on demon plane ic, all samples */
+/* flag = 1 half-sweep of colour p on demon plane ic, all samples; with
+ * g.tma and tm->ok the demon tiles are staged by TMA */
 cudaError_t micsa_launch_sweep_micsa(const micsa_geo &g, int p, int ic,
                                      uint32_t *spin, uint32_t *d0, uint32_t *d1,
                                      const uint8_t *jb, const int *walk,
-                                     cudaStream_t st);
+                                     const micsa_tma *tm, cudaStream_t st);
 /* flag = 0 half-sweep of colour p with random words rnd[(k*P + i)*W + w] */
 cudaError_t micsa_launch_sweep_metropolis(const micsa_geo &g, int p,
                                           uint32_t *spin, const uint8_t *jb,
