@@ -69,3 +69,40 @@ def test_driver_rejects_bad_input(workdir):
     p = subprocess.run([micsa.DRIVER_PATH] + argv, cwd=workdir, stdout=subprocess.PIPE,
                        stderr=subprocess.STDOUT, text=True)
     assert p.returncode != 0 and "multiple of 8" in p.stdout
+
+
+def test_driver_observable_files(workdir):
+    """MICSA_OBSERVABLES=1: evol_q.txt, evol_C4.txt and evol_xi.txt against
+    the scalar oracle of q and C4 on the spins of the run's own conf.<t>
+    records, and the correlation lengths of that C4."""
+    import json
+    import numpy as np
+    import oracle
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "L16_NR64_2s_nc6.json")))
+    cfg = dict(g["cfg"])
+    L, nr = cfg["L"], cfg["nr"]
+    V, nd = L ** 3, L // 2 + 1
+    env = dict(os.environ, MICSA_OBSERVABLES="1")
+    runs.run_program(micsa.DRIVER_PATH, cfg, workdir, env=env)
+    spin_off, nsb = runs.conf_layout(L, nr)
+    for b in range(cfg["nbits"]):
+        sd = os.path.join(workdir, "I000", "BIT%03d" % b)
+        qlines = [l.split() for l in open(os.path.join(sd, "evol_q.txt"))]
+        c4lines = [l.split() for l in open(os.path.join(sd, "evol_C4.txt"))]
+        xilines = [l.split() for l in open(os.path.join(sd, "evol_xi.txt"))]
+        assert [int(l[0]) for l in qlines] == runs.measured(cfg)
+        for k, t in enumerate(runs.measured(cfg)):
+            uu = np.zeros((nr, V), np.uint8)
+            for r in range(nr):
+                with open(os.path.join(sd, "R%02d" % r, "conf.%016d" % t), "rb") as f:
+                    c = f.read()
+                uu[r] = np.unpackbits(np.frombuffer(c[spin_off:spin_off + nsb], np.uint8),
+                                      bitorder="little")[:V]
+            q, c4 = oracle.overlap_c4(L, nr, uu)
+            assert [int(x) for x in qlines[k][1:]] == list(q), (b, t)
+            got = {int(l[1]): int(l[2]) for l in c4lines if int(l[0]) == t}
+            assert got == {d: int(c4[:, :, d].sum()) for d in range(nd)}, (b, t)
+            _, x12, x23 = micsa.correlation_lengths(L, c4)
+            assert xilines[k][0] == str(t)
+            assert abs(float(xilines[k][1]) - x12) <= 1e-9 * abs(x12) + 1e-12
+            assert abs(float(xilines[k][2]) - x23) <= 1e-9 * abs(x23) + 1e-12
