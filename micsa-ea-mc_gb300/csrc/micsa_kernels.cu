@@ -91,11 +91,6 @@ template <> struct hint<4> {
 __device__ __forceinline__ void prefetch_l2(const uint32_t *a) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
 }
-__device__ __forceinline__ uint32_t ld_byte_keep(const uint8_t *a, uint64_t pol) {
-  uint32_t v;
-  asm("ld.global.nc.L2::cache_hint.u8 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
-  return v;
-}
 
 /* ------------------------------------------------------------ geometry */
 struct site_xyz { int x, y, z; };
@@ -1027,6 +1022,7 @@ int micsa_sweep_zc_candidates(int L, int *out, int max) {
  * 32 streams' words into device words of the sites (walk translation 0). */
 constexpr int REFRESH_REC = 120;
 constexpr uint64_t REFRESH_LCG_A = 3202034522624059733ULL; /* random_generator.h:66 */
+
 
 __device__ __forceinline__ uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
 
