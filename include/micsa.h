@@ -156,13 +156,16 @@ int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0,
 int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration_ms);
 
 /* Text line describing the launch shape the context's autotuner chose at
- * creation: "zc=<z planes per thread> pd=<prefetch distance> split=<0: one
+ * creation: "zc=<z planes per thread> pd=<L2 prefetch distance> split=<0: one
  * launch for all samples, 1: sample-major, one launch per sample>
- * occ=<blocks per SM the registers are allocated for> | <zc>/<pd>/<split>/
- * <occ>:<ms per half-sweep> ...".  The environment variables MICSA_SWEEP_ZC,
- * MICSA_SWEEP_PD, MICSA_SWEEP_SPLIT and MICSA_SWEEP_OCC, read by micsa_create,
- * pin the shape and skip the timing (no candidates listed then).  The reference has fixed launch geometry
- * (calculate_blocks, ini.c:580-602). */
+ * occ=<blocks per SM the registers are allocated for> load=<direct | tma:
+ * demon tiles staged by TMA | async: operands double-buffered by cp.async> |
+ * <zc>/<pd>/<split>/<occ>/<load 0|1|2>:<ms per half-sweep> ...".  The
+ * environment variables MICSA_SWEEP_ZC, MICSA_SWEEP_PD, MICSA_SWEEP_SPLIT,
+ * MICSA_SWEEP_OCC, MICSA_SWEEP_TMA and MICSA_SWEEP_ASYNC, read by
+ * micsa_create, pin the shape and skip the timing (no candidates listed
+ * then).  The reference has fixed launch geometry (calculate_blocks,
+ * ini.c:580-602). */
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n);
 
 /* Spin energies computed without allocating any device memory; this entry

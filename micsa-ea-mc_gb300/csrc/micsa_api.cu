@@ -20,7 +20,7 @@
 #include "micsa_jump.h"
 #include "micsa_kernels.cuh"
 
-#define MICSA_TUNE_MAX 96
+#define MICSA_TUNE_MAX 160
 
 struct micsa_ctx {
   micsa_config cfg;
@@ -252,10 +252,11 @@ int autotune(micsa_ctx *ctx) {
     g.zc = zc;
     g.pd = pd;
     const char *es = getenv("MICSA_SWEEP_SPLIT"), *eo = getenv("MICSA_SWEEP_OCC"),
-               *et = getenv("MICSA_SWEEP_TMA");
+               *et = getenv("MICSA_SWEEP_TMA"), *ea = getenv("MICSA_SWEEP_ASYNC");
     ctx->split = es && atoi(es) && g.ns > 1;
     g.occ = eo && atoi(eo) == 4 ? 4 : 3;
     g.tma = et && atoi(et) && ctx->tma.ok;
+    g.async = ea && atoi(ea) && g.W == 2 && !g.tma;
     ctx->ntune = 0;
     return MICSA_OK;
   }
@@ -263,20 +264,24 @@ int autotune(micsa_ctx *ctx) {
   MICSA_CK(cudaEventCreate(&e0));
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
-  int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, best_tma = 0, n = 0;
+  int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, best_tma = 0;
+  int best_async = 0, n = 0;
   const int reps = 2;
   const int nocc = g.W % 4 ? 2 : 1; /* the 4-blocks variant exists for VW <= 2 */
-  for (int tm = 0; tm < (ctx->tma.ok ? 2 : 1); tm++)
+  /* tm: 0 direct loads, 1 TMA-staged demon tiles, 2 cp.async double buffer (W = 2) */
+  for (int tm = 0; tm < (g.W == 2 ? 3 : (ctx->tma.ok ? 2 : 1)); tm++)
   for (int oc = 0; oc < nocc; oc++)
   for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
   for (int c = 0; c < nz; c++)
     for (int d = 0; d < 3; d++) {
       if (pds[d] && pds[d] >= zcs[c]) continue; /* prefetch only within a slab */
-      if (tm && zcs[c] > 4) continue;              /* staged tiles: at most 4 planes */
+      if (tm == 1 && (!ctx->tma.ok || zcs[c] > 4)) continue; /* staged tiles: <= 4 planes */
+      if (tm == 2 && pds[d]) continue;                         /* no L2 prefetch there */
       g.zc = zcs[c];
       g.pd = pds[d];
       g.occ = oc ? 4 : 3;
-      g.tma = tm;
+      g.tma = tm == 1;
+      g.async = tm == 2;
       for (int rep = -1; rep < reps; rep++) { /* rep -1: warm-up */
         if (rep == 0) MICSA_CK(cudaEventRecord(e0, ctx->stream));
         MICSA_CK(launch_halves(ctx, g, sp, 0, g.nc, nullptr)); /* one iteration's order */
@@ -291,7 +296,7 @@ int autotune(micsa_ctx *ctx) {
         ctx->tune_pd[n] = g.pd;
         ctx->tune_split[n] = sp;
         ctx->tune_occ[n] = g.occ;
-        ctx->tune_tma[n] = g.tma;
+        ctx->tune_tma[n] = tm;
         ctx->tune_ms[n] = per;
         n++;
       }
@@ -302,6 +307,7 @@ int autotune(micsa_ctx *ctx) {
         best_split = sp;
         best_occ = g.occ;
         best_tma = g.tma;
+        best_async = g.async;
       }
     }
   ctx->ntune = n;
@@ -310,6 +316,7 @@ int autotune(micsa_ctx *ctx) {
   ctx->split = best_split;
   g.occ = best_occ;
   g.tma = best_tma;
+  g.async = best_async;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return MICSA_OK;
@@ -361,6 +368,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.pd = 0;
   g.occ = 3;
   g.tma = 0;
+  g.async = 0;
   g.s0 = 0;
   g.H = s.H;
   g.active = nullptr;
@@ -432,8 +440,9 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d tma=%d |", ctx->g.zc, ctx->g.pd,
-                   ctx->split, ctx->g.occ, ctx->g.tma);
+  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s |", ctx->g.zc, ctx->g.pd,
+                   ctx->split, ctx->g.occ,
+                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : "direct"));
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
     k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],
                   ctx->tune_pd[c], ctx->tune_split[c], ctx->tune_occ[c], ctx->tune_tma[c],

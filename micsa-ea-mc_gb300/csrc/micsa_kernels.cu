@@ -529,6 +529,189 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
   }
 }
 
+/* ------------------------------------------- sweep with cp.async staging */
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, uint64_t pol) {
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;"
+               ::"r"(smem_addr(dst)), "l"(src), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src, uint64_t pol) {
+  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;"
+               ::"r"(smem_addr(dst)), "l"(src), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src, uint64_t pol) {
+  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;"
+               ::"r"(smem_addr(dst)), "l"(src), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int NPEND> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(NPEND) : "memory");
+}
+
+constexpr int ASYNC_ITEMS = 7; /* own, up, y+1, y-1, D0, D1, {x-neighbour word pair, couplings} */
+
+/* The micSA half-sweep of k_sweep (VW = 2, one word group per site) with its
+ * per-step operands double-buffered in shared memory: while a thread
+ * computes z step t, its copies for step t+1 are in flight (cp.async), so
+ * the latency of the next loads overlaps the arithmetic of this step.  Each
+ * thread copies and reads only its own slots (item-major layout,
+ * [stage][item][thread] x 16 bytes: conflict-free), waiting on its own copy
+ * groups -- no barrier.  Prefetching a step is safe: a thread's own spins
+ * and demon words are written only by that thread, the other colour and the
+ * couplings are read-only during a half-sweep. */
+template <int MINB>
+__global__ void __launch_bounds__(TPB, MINB)
+k_sweep_async(const micsa_geo g, const int p, const int ic, const int ytiles, const int zc,
+              uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
+              uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
+              const int *__restrict__ walk) {
+  constexpr int VW = 2, N = 4;
+  const uint32_t L = g.L, Lh = g.Lh, W = g.W; /* W == 2 */
+  const uint32_t by = blockIdx.y;
+  const uint32_t tile = by % ytiles, s = by / ytiles;
+  if (micsa_frozen(g, (int)s)) return;
+  const uint32_t y = tile * blockDim.y + threadIdx.y;
+  if (y >= L) return;
+  const uint32_t xa = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const uint32_t plane = L * Lh;
+  const uint32_t z0 = blockIdx.z * zc;
+  const uint32_t row = y * Lh + xa;
+  const uint32_t rowN = (y + 1 == L) ? xa : row + Lh;
+  const uint32_t rowS = (y == 0) ? row + (L - 1) * Lh : row - Lh;
+  const uint32_t rowXp = (xa + 2 == Lh) ? row + 2 - Lh : row + 2;
+  const uint32_t rowXm = (xa == 0) ? row + Lh - 1 : row - 1;
+  const size_t P = (size_t)g.P;
+  uint32_t *mine = spin + (size_t)(s * 2 + p) * P * W;
+  const uint32_t *oth = spin + (size_t)(s * 2 + (p ^ 1)) * P * W;
+  const uint8_t *jbp = jb + (size_t)(s * 2 + p) * P;
+  const uint64_t keep = l2_keep(), strm = l2_stream();
+
+  uint32_t drowA = row, drowB = row + 1, zd = z0;
+  bool dpair = true;
+  {
+    const int k = __ldg(walk + s);
+    const int sh = ((p == 0) == (ic < 3)) ? k : -k;
+    const int axis = ic < 3 ? ic : ic - 3;
+    if (axis == 0) {
+      int xd = (int)xa - sh;
+      xd += xd < 0 ? (int)Lh : (xd >= (int)Lh ? -(int)Lh : 0);
+      const int xe = (xd + 1 == (int)Lh) ? 0 : xd + 1;
+      drowA = y * Lh + (uint32_t)xd;
+      drowB = y * Lh + (uint32_t)xe;
+      dpair = !(sh & 1);
+    } else if (axis == 1) {
+      int yd = (int)y - 2 * sh;
+      yd += yd < 0 ? (int)L : (yd >= (int)L ? -(int)L : 0);
+      drowA = (uint32_t)yd * Lh + xa;
+      drowB = drowA + 1;
+    } else {
+      int t = (int)z0 - 2 * sh;
+      t += t < 0 ? (int)L : (t >= (int)L ? -(int)L : 0);
+      zd = (uint32_t)t;
+    }
+  }
+  const size_t dbase = ((size_t)(s * 2 + p) * g.nc + ic) * P * W;
+  uint32_t *q0b = d0 + dbase, *q1b = d1 + dbase;
+
+  extern __shared__ __align__(16) uint4 sbuf[];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  auto slot = [&](int st, int item) -> uint4 * { return sbuf + (st * ASYNC_ITEMS + item) * TPB + tid; };
+  /* the copies of z step t into stage t & 1 */
+  auto issue = [&](uint32_t t) {
+    const int st = (int)(t & 1);
+    const uint32_t z = z0 + t, zo = z * plane, rowoff = (y + z + p) & 1;
+    uint32_t zt = zd + t;
+    zt -= zt >= L ? L : 0;
+    cp_async16(slot(st, 0), mine + (zo + row) * W, keep);
+    cp_async16(slot(st, 1), oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, keep);
+    cp_async16(slot(st, 2), oth + (zo + rowN) * W, keep);
+    cp_async16(slot(st, 3), oth + (zo + rowS) * W, keep);
+    const uint32_t sa = (zt * plane + drowA) * W;
+    if (dpair) {
+      cp_async16(slot(st, 4), q0b + sa, strm);
+      cp_async16(slot(st, 5), q1b + sa, strm);
+    } else {
+      const uint32_t sb = (zt * plane + drowB) * W;
+      cp_async8(slot(st, 4), q0b + sa, strm);
+      cp_async8((uint8_t *)slot(st, 4) + 8, q0b + sb, strm);
+      cp_async8(slot(st, 5), q1b + sa, strm);
+      cp_async8((uint8_t *)slot(st, 5) + 8, q1b + sb, strm);
+    }
+    cp_async8(slot(st, 6), oth + (zo + (rowoff ? rowXp : rowXm)) * W, keep);
+    const size_t jo = zo + row; /* the pair's two coupling bytes, in an aligned word */
+    cp_async4((uint8_t *)slot(st, 6) + 8, jbp + (jo & ~(size_t)3), keep);
+    cp_async_commit();
+  };
+
+  uint32_t vm[N], v0[N];
+  hint<4>::ld_nc(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, vm, keep);
+  hint<4>::ld_nc(oth + (z0 * plane + row) * W, v0, keep);
+  issue(0);
+  uint32_t zdd = zd;
+  for (uint32_t t = 0; t < (uint32_t)zc; t++) {
+    if (t + 1 < (uint32_t)zc) {
+      issue(t + 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    const int st = (int)(t & 1);
+    const uint32_t z = z0 + t, zo = z * plane, rowoff = (y + z + p) & 1;
+    uint32_t own[N], up[N], vn[N], vs[N], a0[N], a1[N];
+    {
+      const uint4 o = *slot(st, 0), u = *slot(st, 1), n = *slot(st, 2), q = *slot(st, 3);
+      const uint4 e0 = *slot(st, 4), e1 = *slot(st, 5);
+      own[0] = o.x; own[1] = o.y; own[2] = o.z; own[3] = o.w;
+      up[0] = u.x; up[1] = u.y; up[2] = u.z; up[3] = u.w;
+      vn[0] = n.x; vn[1] = n.y; vn[2] = n.z; vn[3] = n.w;
+      vs[0] = q.x; vs[1] = q.y; vs[2] = q.z; vs[3] = q.w;
+      a0[0] = e0.x; a0[1] = e0.y; a0[2] = e0.z; a0[3] = e0.w;
+      a1[0] = e1.x; a1[1] = e1.y; a1[2] = e1.z; a1[3] = e1.w;
+    }
+    const uint4 xj = *slot(st, 6);
+    const uint32_t ext[VW] = {xj.x, xj.y};
+    const uint32_t jb2 = (xj.z >> (8 * ((zo + row) & 3))) & 0xffffu;
+#pragma unroll
+    for (int site = 0; site < 2; site++) {
+      const uint32_t jb6 = (jb2 >> (8 * site)) & 0xffu;
+      const uint32_t mE = jmask(jb6, 0), mN = jmask(jb6, 1), mU = jmask(jb6, 2);
+      const uint32_t mO = jmask(jb6, 3), mS = jmask(jb6, 4), mD = jmask(jb6, 5);
+#pragma unroll
+      for (int w = 0; w < VW; w++) {
+        const int o = site * VW + w;
+        const uint32_t cA = v0[w], cB = v0[VW + w], ex = ext[w];
+        const uint32_t nE = site == 0 ? (rowoff ? cB : cA) : (rowoff ? ex : cB);
+        const uint32_t nO = site == 0 ? (rowoff ? cA : ex) : (rowoff ? cB : cA);
+        const uint32_t sw = own[o];
+        const uint32_t f0 = sw ^ nE ^ mE, f1 = sw ^ vn[o] ^ mN, f2 = sw ^ up[o] ^ mU;
+        const uint32_t f3 = sw ^ nO ^ mO, f4 = sw ^ vs[o] ^ mS, f5 = sw ^ vm[o] ^ mD;
+        const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
+        const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+        own[o] = sw ^ isi_update(j1, j2, j3, j4, a0[o], a1[o]);
+      }
+    }
+    hint<4>::st(mine + (zo + row) * W, own, keep);
+    const uint32_t sa = (zdd * plane + drowA) * W;
+    if (dpair) {
+      hint<4>::st(q0b + sa, a0, strm);
+      hint<4>::st(q1b + sa, a1, strm);
+    } else {
+      const uint32_t sb = (zdd * plane + drowB) * W;
+      const uint32_t x0[2] = {a0[0], a0[1]}, x1[2] = {a0[2], a0[3]};
+      const uint32_t y0[2] = {a1[0], a1[1]}, y1[2] = {a1[2], a1[3]};
+      hint<2>::st(q0b + sa, x0, strm);
+      hint<2>::st(q0b + sb, x1, strm);
+      hint<2>::st(q1b + sa, y0, strm);
+      hint<2>::st(q1b + sb, y1, strm);
+    }
+#pragma unroll
+    for (int w = 0; w < N; w++) {
+      vm[w] = v0[w];
+      v0[w] = up[w];
+    }
+    zdd = (zdd + 1 == L) ? 0 : zdd + 1;
+  }
+}
+
 /* ------------------------------------------------------ Philox + LUT bits */
 
 /* Philox4x32-10 (Salmon et al., SC'11): 10 rounds, Weyl key schedule. */
@@ -849,6 +1032,20 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
   const bool tma = micsa && tm && tm->ok && g.tma && G == 1 && g.L % ty == 0 && zc <= 4 &&
                    tm->ty == ty && tm->box_w >= 2 * tx * VW;
   const size_t smem = tma ? (size_t)2 * zc * ty * tm->box_w * 4 + (size_t)zc * 8 : 0;
+  if (VW == 2 && micsa && g.async && G == 1 && !tma) {
+    const size_t sb = (size_t)2 * ASYNC_ITEMS * TPB * 16;
+    cudaError_t e;
+    if (g.occ == 4) {
+      if ((e = cudaFuncSetAttribute(k_sweep_async<B1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sb)) != cudaSuccess) return e;
+      k_sweep_async<B1><<<grid, block, sb, st>>>(g, p, ic, ytiles, zc, spin, d0, d1, jb, walk);
+    } else {
+      if ((e = cudaFuncSetAttribute(k_sweep_async<B0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sb)) != cudaSuccess) return e;
+      k_sweep_async<B0><<<grid, block, sb, st>>>(g, p, ic, ytiles, zc, spin, d0, d1, jb, walk);
+    }
+    return cudaGetLastError();
+  }
   micsa_tma none;
   const micsa_tma &t = tm ? *tm : none;
 #define MICSA_SWEEP(M, WD, B, T)                                                                  \

@@ -30,6 +30,7 @@ struct micsa_geo {
   int pd;     /* L2 prefetch distance of the demon stream, in z steps (0 = off) */
   int occ;    /* sweep variant: 4 = register cap for 4 blocks per SM, else the compiler's */
   int tma;    /* 1: the sweep stages its demon tiles in shared memory by TMA */
+  int async;  /* 1: the sweep double-buffers each step's operands with cp.async (W = 2) */
   int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */

@@ -37,7 +37,7 @@ def test_staged_sweep_matches_oracle(L, nr, nc, ns, split):
                    "MICSA_SWEEP_SPLIT": str(split), "MICSA_SWEEP_OCC": "4", "MICSA_RESIDENT": "0"})
     try:
         ctx = micsa.Context(L, nr, ns, nc)
-        assert "tma=1" in ctx.tuning(), ctx.tuning()
+        assert "load=tma" in ctx.tuning(), ctx.tuning()
     finally:
         _restore(old)
     rng = np.random.default_rng(L + nr + ns)
@@ -50,6 +50,39 @@ def test_staged_sweep_matches_oracle(L, nr, nc, ns, split):
             ctx.upload_demons(s, w0, w1)
         ctx.iterate(iters)
         ctx.synchronize()  # also reports any staged load that timed out
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            for _ in range(iters):
+                oracle.micsa_iteration(L, nr, nc, J, e, o, w0, w1, 8)
+            ge, go = ctx.download_spins(s)
+            g0, g1 = ctx.download_demons(s)
+            assert np.array_equal(ge, e) and np.array_equal(go, o), s
+            assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
+
+
+@pytest.mark.parametrize("L,nc,ns,split,occ", [(32, 6, 2, 0, 4), (40, 3, 1, 0, 3), (64, 6, 2, 1, 4),
+                                               (96, 5, 2, 1, 3)])
+def test_async_staged_sweep_matches_oracle(L, nc, ns, split, occ):
+    """The cp.async double-buffered sweep (64 replicas, one 8-byte vector per
+    site), pinned on, against the oracle over every walk shift."""
+    nr = 64
+    old = _pinned({"MICSA_SWEEP_ZC": "4", "MICSA_SWEEP_PD": "0", "MICSA_SWEEP_ASYNC": "1",
+                   "MICSA_SWEEP_SPLIT": str(split), "MICSA_SWEEP_OCC": str(occ),
+                   "MICSA_RESIDENT": "0"})
+    try:
+        ctx = micsa.Context(L, nr, ns, nc)
+        assert "load=async" in ctx.tuning(), ctx.tuning()
+    finally:
+        _restore(old)
+    rng = np.random.default_rng(7 * L + ns)
+    st = random_state(rng, L, nr, nc, ns)
+    iters = L // 2 + 3
+    with ctx:
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            ctx.upload_couplings(s, J)
+            ctx.upload_spins(s, e, o)
+            ctx.upload_demons(s, w0, w1)
+        ctx.iterate(iters)
+        ctx.synchronize()
         for s, (J, e, o, w0, w1, _) in enumerate(st):
             for _ in range(iters):
                 oracle.micsa_iteration(L, nr, nc, J, e, o, w0, w1, 8)
