@@ -106,3 +106,62 @@ def test_driver_observable_files(workdir):
             assert xilines[k][0] == str(t)
             assert abs(float(xilines[k][1]) - x12) <= 1e-9 * abs(x12) + 1e-12
             assert abs(float(xilines[k][2]) - x23) <= 1e-9 * abs(x23) + 1e-12
+
+
+def _small_cfg(**kw):
+    cfg = dict(L=16, nr=32, nbits=1, nc=6, nterm=0, maxtime=8, times=[1, 2, 4, 8], seed_J=5,
+               seed_u=7, seed_MC0=11)
+    cfg.update(kw)
+    return cfg
+
+
+def test_driver_lock_refuses_a_second_run(workdir):
+    """create_running (io.c:1016-1047): a `running` lock in the sample folder
+    stops a second program on the same folder."""
+    import subprocess
+    argv = runs.write_inputs(workdir, _small_cfg())
+    os.makedirs(os.path.join(workdir, "I000"), exist_ok=True)
+    open(os.path.join(workdir, "I000", "running"), "w").close()
+    p = subprocess.run([micsa.DRIVER_PATH] + argv, cwd=workdir, stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=300)
+    assert p.returncode != 0 and "exists" in p.stdout, p.stdout[-2000:]
+
+
+def test_driver_changentimes_replaces_the_measurements(workdir):
+    """changentimes.in ("n t_1 ... t_n") replaces the list of measurement times."""
+    cfg = _small_cfg()
+    runs.write_inputs(workdir, cfg)
+    os.makedirs(os.path.join(workdir, "I000"), exist_ok=True)
+    with open(os.path.join(workdir, "I000", "changentimes.in"), "w") as f:
+        f.write("2\n1\n4\n")
+    import subprocess
+    argv = runs.write_inputs(workdir, cfg)
+    p = subprocess.run([micsa.DRIVER_PATH] + argv, cwd=workdir, stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=300)
+    assert p.returncode == 0, p.stdout[-2000:]
+    lines = open(os.path.join(workdir, "I000", "BIT000", "evol_E_spins.txt")).read().splitlines()
+    assert [int(l.split()[0]) for l in lines] == [1, 4]
+
+
+def test_driver_sigterm_stops_between_iterations(workdir):
+    """A SIGTERM is recorded by the handler and acted on between iterations
+    (stop_run, io.c:970-994): exit status 1, the error file names the signal,
+    the running lock is gone."""
+    import signal
+    import subprocess
+    import time
+    cfg = _small_cfg(maxtime=1 << 26, times=[1 << 26])
+    argv = runs.write_inputs(workdir, cfg)
+    p = subprocess.Popen([micsa.DRIVER_PATH] + argv, cwd=workdir, stdout=subprocess.PIPE,
+                         stderr=subprocess.STDOUT, text=True)
+    lock = os.path.join(workdir, "I000", "running")
+    t0 = time.time()
+    while not os.path.exists(lock) and time.time() - t0 < 120 and p.poll() is None:
+        time.sleep(0.05)
+    assert os.path.exists(lock), "the run never took its lock"
+    time.sleep(0.5)
+    p.send_signal(signal.SIGTERM)
+    out, _ = p.communicate(timeout=300)
+    assert p.returncode == 1, out[-2000:]
+    assert "Received SIGTERM" in open(os.path.join(workdir, "I000", "error")).read()
+    assert not os.path.exists(lock)
