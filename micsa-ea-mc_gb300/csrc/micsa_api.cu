@@ -12,8 +12,11 @@
 #include <string.h>
 
 #include <atomic>
+#include <map>
+#include <mutex>
 #include <new>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "micsa.h"
@@ -49,6 +52,7 @@ struct micsa_ctx {
   int tune_split[MICSA_TUNE_MAX] = {0}, tune_occ[MICSA_TUNE_MAX] = {0};
   int tune_tma[MICSA_TUNE_MAX] = {0};
   double tune_ms[MICSA_TUNE_MAX] = {0};
+  int tune_cached = 0; /* the shape came from an earlier context's timing */
   /* demon refresh on the device: jump tables of one segment length */
   micsa_refresh_plan plan = {};
   uint64_t *plan_lcg = nullptr, *plan_xo = nullptr, *plan_fib = nullptr;
@@ -227,12 +231,30 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
   return e;
 }
 
+/* Launch shapes chosen so far in this process, by (device, L, nr, samples,
+ * nc, TMA maps usable): a context of a shape timed before takes the earlier
+ * choice and table instead of timing again, so batches and servers that open
+ * many contexts of a few shapes pay for each shape once. */
+struct tune_entry {
+  int zc, pd, split, occ, tma, async, n;
+  std::vector<int> zcs, pds, splits, occs, tmas;
+  std::vector<double> ms;
+};
+std::mutex tune_mu;
+std::map<std::tuple<int, int, int, int, int, int>, tune_entry> tune_cache;
+
+std::tuple<int, int, int, int, int, int> tune_key(const micsa_ctx *ctx) {
+  return std::make_tuple(ctx->cfg.device, ctx->g.L, ctx->cfg.nr, ctx->g.ns, ctx->g.nc,
+                         ctx->tma.ok ? 1 : 0);
+}
+
 /* Launch-shape autotuner: time the half-sweeps of whole iterations, in their
  * real launch order, for every z-chunk length that divides L, prefetch
  * distance, sample order (merged or sample-major) and register budget, on the
  * freshly zeroed buffers; keep the fastest, then zero the buffers again.  Results do not
  * depend on the choice (each site is updated by exactly one thread either
- * way); only the speed does. */
+ * way); only the speed does.  MICSA_TUNE_CACHE=0 times every context afresh
+ * instead of reusing the process's earlier choice for the same shape. */
 int autotune(micsa_ctx *ctx) {
   micsa_geo &g = ctx->g;
   int zcs[8];
@@ -259,6 +281,32 @@ int autotune(micsa_ctx *ctx) {
     g.async = ea && atoi(ea) && g.W == 2 && !g.tma;
     ctx->ntune = 0;
     return MICSA_OK;
+  }
+  const char *ec = getenv("MICSA_TUNE_CACHE");
+  const bool use_cache = !(ec && !strcmp(ec, "0"));
+  if (use_cache) {
+    std::lock_guard<std::mutex> lk(tune_mu);
+    auto it = tune_cache.find(tune_key(ctx));
+    if (it != tune_cache.end()) {
+      const tune_entry &t = it->second;
+      g.zc = t.zc;
+      g.pd = t.pd;
+      ctx->split = t.split;
+      g.occ = t.occ;
+      g.tma = t.tma;
+      g.async = t.async;
+      ctx->ntune = t.n;
+      for (int c = 0; c < t.n; c++) {
+        ctx->tune_zc[c] = t.zcs[c];
+        ctx->tune_pd[c] = t.pds[c];
+        ctx->tune_split[c] = t.splits[c];
+        ctx->tune_occ[c] = t.occs[c];
+        ctx->tune_tma[c] = t.tmas[c];
+        ctx->tune_ms[c] = t.ms[c];
+      }
+      ctx->tune_cached = 1;
+      return MICSA_OK;
+    }
   }
   cudaEvent_t e0, e1;
   MICSA_CK(cudaEventCreate(&e0));
@@ -319,6 +367,24 @@ int autotune(micsa_ctx *ctx) {
   g.async = best_async;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (use_cache) {
+    tune_entry t;
+    t.zc = g.zc;
+    t.pd = g.pd;
+    t.split = ctx->split;
+    t.occ = g.occ;
+    t.tma = g.tma;
+    t.async = g.async;
+    t.n = n;
+    t.zcs.assign(ctx->tune_zc, ctx->tune_zc + n);
+    t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
+    t.splits.assign(ctx->tune_split, ctx->tune_split + n);
+    t.occs.assign(ctx->tune_occ, ctx->tune_occ + n);
+    t.tmas.assign(ctx->tune_tma, ctx->tune_tma + n);
+    t.ms.assign(ctx->tune_ms, ctx->tune_ms + n);
+    std::lock_guard<std::mutex> lk(tune_mu);
+    tune_cache.emplace(tune_key(ctx), std::move(t)); /* the first timing of a shape stays */
+  }
   return MICSA_OK;
 }
 
@@ -440,9 +506,10 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s |", ctx->g.zc, ctx->g.pd,
+  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s%s |", ctx->g.zc, ctx->g.pd,
                    ctx->split, ctx->g.occ,
-                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : "direct"));
+                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : "direct"),
+                   ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
     k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],
                   ctx->tune_pd[c], ctx->tune_split[c], ctx->tune_occ[c], ctx->tune_tma[c],
