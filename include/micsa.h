@@ -159,13 +159,14 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
  * creation: "zc=<z planes per thread> pd=<L2 prefetch distance> split=<0: one
  * launch for all samples, 1: sample-major, one launch per sample>
  * occ=<blocks per SM the registers are allocated for> load=<direct | tma:
- * demon tiles staged by TMA | async: operands double-buffered by cp.async> |
- * <zc>/<pd>/<split>/<occ>/<load 0|1|2>:<ms per half-sweep> ...", with
+ * demon tiles staged by TMA | async: operands double-buffered by cp.async |
+ * pipe: each z step's loads issued one step ahead into registers> |
+ * <zc>/<pd>/<split>/<occ>/<load 0|1|2|3>:<ms per half-sweep> ...", with
  * " cached" before the "|" when the choice and its table were taken over
  * from an earlier context of the same device, L, nr, samples and nc in this
  * process (MICSA_TUNE_CACHE=0 times every context instead).  The
  * environment variables MICSA_SWEEP_ZC, MICSA_SWEEP_PD, MICSA_SWEEP_SPLIT,
- * MICSA_SWEEP_OCC, MICSA_SWEEP_TMA and MICSA_SWEEP_ASYNC, read by
+ * MICSA_SWEEP_OCC, MICSA_SWEEP_TMA, MICSA_SWEEP_ASYNC and MICSA_SWEEP_PIPE, read by
  * micsa_create, pin the shape and skip the timing (no candidates listed
  * then).  The reference has fixed launch geometry (calculate_blocks,
  * ini.c:580-602). */

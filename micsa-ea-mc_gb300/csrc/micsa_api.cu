@@ -131,17 +131,6 @@ int check_cfg(const micsa_config *c, char *msg, size_t n) {
   return MICSA_OK;
 }
 
-/* block-edge rotations of a reference word toward -x, -y, -z (RotateO/S/D,
- * main.cu:732-742): bit of block b receives the bit of block b-1 along the
- * axis. */
-uint64_t rot_back(int d, uint64_t v) {
-  switch (d) {
-    case 3: { const uint64_t m = 0x8888888888888888ULL; return ((v & m) >> 3) | ((v & ~m) << 1); }
-    case 4: { const uint64_t m = 0xF000F000F000F000ULL; return ((v & m) >> 12) | ((v & ~m) << 4); }
-    default: { const uint64_t m = 0xFFFF000000000000ULL; return ((v & m) >> 48) | ((v & ~m) << 16); }
-  }
-}
-
 int set_device(micsa_ctx *ctx) {
   MICSA_CK(cudaSetDevice(ctx->cfg.device));
   return MICSA_OK;
@@ -236,7 +225,7 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
  * choice and table instead of timing again, so batches and servers that open
  * many contexts of a few shapes pay for each shape once. */
 struct tune_entry {
-  int zc, pd, split, occ, tma, async, n;
+  int zc, pd, split, occ, tma, async, pipe, n;
   std::vector<int> zcs, pds, splits, occs, tmas;
   std::vector<double> ms;
 };
@@ -274,11 +263,14 @@ int autotune(micsa_ctx *ctx) {
     g.zc = zc;
     g.pd = pd;
     const char *es = getenv("MICSA_SWEEP_SPLIT"), *eo = getenv("MICSA_SWEEP_OCC"),
-               *et = getenv("MICSA_SWEEP_TMA"), *ea = getenv("MICSA_SWEEP_ASYNC");
+               *et = getenv("MICSA_SWEEP_TMA"), *ea = getenv("MICSA_SWEEP_ASYNC"),
+               *ep2 = getenv("MICSA_SWEEP_PIPE");
     ctx->split = es && atoi(es) && g.ns > 1;
-    g.occ = eo && atoi(eo) == 4 ? 4 : 3;
     g.tma = et && atoi(et) && ctx->tma.ok;
     g.async = ea && atoi(ea) && g.W == 2 && !g.tma;
+    g.pipe = ep2 && atoi(ep2) && !g.tma && !g.async;
+    const int oc = eo ? atoi(eo) : 3;
+    g.occ = g.pipe ? (oc == 2 ? 2 : 3) : (oc == 4 ? 4 : 3);
     ctx->ntune = 0;
     return MICSA_OK;
   }
@@ -295,6 +287,7 @@ int autotune(micsa_ctx *ctx) {
       g.occ = t.occ;
       g.tma = t.tma;
       g.async = t.async;
+      g.pipe = t.pipe;
       ctx->ntune = t.n;
       for (int c = 0; c < t.n; c++) {
         ctx->tune_zc[c] = t.zcs[c];
@@ -313,31 +306,48 @@ int autotune(micsa_ctx *ctx) {
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
   int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, best_tma = 0;
-  int best_async = 0, n = 0;
-  const int reps = 2;
+  int best_async = 0, best_pipe = 0, n = 0;
+  const int reps = 3;
   const int nocc = g.W % 4 ? 2 : 1; /* the 4-blocks variant exists for VW <= 2 */
-  /* tm: 0 direct loads, 1 TMA-staged demon tiles, 2 cp.async double buffer (W = 2) */
-  for (int tm = 0; tm < (g.W == 2 ? 3 : (ctx->tma.ok ? 2 : 1)); tm++)
+  /* tm: 0 direct loads, 1 TMA-staged demon tiles, 2 cp.async double buffer (W = 2),
+   * 3 loads pipelined one step ahead in registers (register budget for 3 or 2
+   * blocks per SM instead of 3 or 4) */
+  for (int tm = 0; tm < 4; tm++)
   for (int oc = 0; oc < nocc; oc++)
   for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
   for (int c = 0; c < nz; c++)
     for (int d = 0; d < 3; d++) {
       if (pds[d] && pds[d] >= zcs[c]) continue; /* prefetch only within a slab */
       if (tm == 1 && (!ctx->tma.ok || zcs[c] > 4)) continue; /* staged tiles: <= 4 planes */
-      if (tm == 2 && pds[d]) continue;                         /* no L2 prefetch there */
+      if (tm == 2 && (g.W != 2 || pds[d])) continue;          /* no L2 prefetch there */
       g.zc = zcs[c];
       g.pd = pds[d];
-      g.occ = oc ? 4 : 3;
+      g.occ = tm == 3 ? (oc ? 2 : 3) : (oc ? 4 : 3);
       g.tma = tm == 1;
       g.async = tm == 2;
-      for (int rep = -1; rep < reps; rep++) { /* rep -1: warm-up */
-        if (rep == 0) MICSA_CK(cudaEventRecord(e0, ctx->stream));
-        MICSA_CK(launch_halves(ctx, g, sp, 0, g.nc, nullptr)); /* one iteration's order */
-      }
-      MICSA_CK(cudaEventRecord(e1, ctx->stream));
-      MICSA_CK(cudaEventSynchronize(e1));
+      g.pipe = tm == 3;
+      /* one iteration's half-sweeps in their launch order, captured and
+       * replayed as a graph the way micsa_iterate runs them: timed launch by
+       * launch, small lattices would measure the host's launch rate */
+      cudaGraph_t gr = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      const cudaError_t le = launch_halves(ctx, g, sp, 0, g.nc, nullptr);
+      const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &gr);
+      MICSA_CK(le);
+      MICSA_CK(ce);
+      const cudaError_t ie = cudaGraphInstantiate(&ge, gr, 0);
+      cudaGraphDestroy(gr);
+      MICSA_CK(ie);
       float ms = 0;
-      MICSA_CK(cudaEventElapsedTime(&ms, e0, e1));
+      cudaError_t te = cudaGraphLaunch(ge, ctx->stream); /* warm-up */
+      if (te == cudaSuccess) te = cudaEventRecord(e0, ctx->stream);
+      for (int rep = 0; rep < reps && te == cudaSuccess; rep++) te = cudaGraphLaunch(ge, ctx->stream);
+      if (te == cudaSuccess) te = cudaEventRecord(e1, ctx->stream);
+      if (te == cudaSuccess) te = cudaEventSynchronize(e1);
+      if (te == cudaSuccess) te = cudaEventElapsedTime(&ms, e0, e1);
+      cudaGraphExecDestroy(ge);
+      MICSA_CK(te);
       const double per = ms / (2.0 * g.nc * reps);
       if (n < MICSA_TUNE_MAX) {
         ctx->tune_zc[n] = g.zc;
@@ -356,6 +366,7 @@ int autotune(micsa_ctx *ctx) {
         best_occ = g.occ;
         best_tma = g.tma;
         best_async = g.async;
+        best_pipe = g.pipe;
       }
     }
   ctx->ntune = n;
@@ -365,6 +376,7 @@ int autotune(micsa_ctx *ctx) {
   g.occ = best_occ;
   g.tma = best_tma;
   g.async = best_async;
+  g.pipe = best_pipe;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (use_cache) {
@@ -375,6 +387,7 @@ int autotune(micsa_ctx *ctx) {
     t.occ = g.occ;
     t.tma = g.tma;
     t.async = g.async;
+    t.pipe = g.pipe;
     t.n = n;
     t.zcs.assign(ctx->tune_zc, ctx->tune_zc + n);
     t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
@@ -435,6 +448,12 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.occ = 3;
   g.tma = 0;
   g.async = 0;
+  g.pipe = 0;
+  {
+    /* MICSA_PDL=0: plain launches of the sweeps */
+    const char *e = getenv("MICSA_PDL");
+    g.pdl = !(e && !strcmp(e, "0"));
+  }
   g.s0 = 0;
   g.H = s.H;
   g.active = nullptr;
@@ -508,7 +527,7 @@ int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
   int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s%s |", ctx->g.zc, ctx->g.pd,
                    ctx->split, ctx->g.occ,
-                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : "direct"),
+                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : "direct")),
                    ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
     k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],
@@ -578,32 +597,16 @@ int micsa_set_lut(micsa_ctx *ctx, const void *lut, size_t bytes) {
 int micsa_upload_couplings(micsa_ctx *ctx, int sample, const uint64_t *J) {
   if (!ctx || !J) return fail(ctx, MICSA_ERR_ARG, "null argument");
   int rc = check_sample(ctx, sample);
-  if (rc || (rc = set_device(ctx))) return rc;
+  if (rc || (rc = set_device(ctx)) || (rc = ensure_stage(ctx))) return rc;
   const micsa_geo &g = ctx->g;
-  const int L = g.L, m = L / 4, mh = m / 2;
-  /* per site: bit d = bond in direction d, taken from the reference words
-   * the way d_oneMCstepBN consumes them (main.cu:910-927): forward words
-   * bit-aligned, backward words realigned by the block-edge rotation */
-  std::vector<uint8_t> jb((size_t)(2 * g.P), 0);
-  for (int p = 0; p < 2; p++)
-    for (int64_t h = 0; h < g.H; h++) {
-      const int a2 = (int)(h % mh), b = (int)((h / mh) % m), c = (int)(h / ((int64_t)mh * m));
-      const int a = 2 * a2 + ((b + c + p) & 1);
-      const int wrap[6] = {0, 0, 0, a == 0, b == 0, c == 0};
-      uint64_t w[6];
-      for (int d = 0; d < 6; d++) {
-        w[d] = J[((int64_t)p * 6 + d) * g.H + h];
-        if (wrap[d]) w[d] = rot_back(d, w[d]);
-      }
-      for (int bit = 0; bit < 64; bit++) {
-        const int x = (bit & 3) * m + a, y = ((bit >> 2) & 3) * m + b, z = (bit >> 4) * m + c;
-        uint8_t v = 0;
-        for (int d = 0; d < 6; d++) v |= (uint8_t)(((w[d] >> bit) & 1) << d);
-        jb[(size_t)p * g.P + ((int64_t)z * L + y) * g.Lh + (x >> 1)] = v;
-      }
-    }
-  MICSA_CK(cudaMemcpyAsync(ctx->jb + (int64_t)sample * 2 * g.P, jb.data(), jb.size(),
-                           cudaMemcpyHostToDevice, ctx->stream));
+  /* the 12*H reference words go up as they are; one bond byte per site is
+   * built on the device (bit d = bond in direction d, taken from the words
+   * the way d_oneMCstepBN consumes them, main.cu:910-927) */
+  MICSA_CK(cudaMemcpyAsync(ctx->stage, J, 12 * 8 * (size_t)g.H, cudaMemcpyHostToDevice,
+                           ctx->stream));
+  MICSA_CK(micsa_launch_couplings_from_ref(g, ctx->stage, ctx->jb + (int64_t)sample * 2 * g.P,
+                                           ctx->stream));
+  ctx->launches++;
   MICSA_CK(cudaStreamSynchronize(ctx->stream));
   ctx->have_j[sample] = 1;
   return MICSA_OK;
@@ -706,9 +709,18 @@ int refresh_into(micsa_ctx *ctx, int first, int count, void *prc, void *xo, cons
   micsa_xoshiro_t *X = (micsa_xoshiro_t *)xo;
   const int64_t nw = 2 * g.H * g.nc, nstreams = (int64_t)count * g.nr;
   const size_t words = (size_t)nstreams * MICSA_STREAM_REC;
-  /* segments of 32 words (2048 draws), shorter when the call has few warps */
-  int wps = 32;
-  while (wps > 2 && (int64_t)count * g.W * ((nw + wps - 1) / wps) < 4096) wps >>= 1;
+  /* segments of 48 words (3072 draws per lane) while that still gives 1024
+   * warps, else 32, else 16: each segment's start costs a fixed jump (about
+   * 17k instructions per lane), and small calls are latency-bound anyway --
+   * measured on GB300 over 8 ... 256 words for L = 16 ... 160.
+   * MICSA_REFRESH_WPS pins the length */
+  int wps = 48;
+  while (wps > 16 && (int64_t)count * g.W * ((nw + wps - 1) / wps) < 1024) wps -= 16;
+  if (const char *e = getenv("MICSA_REFRESH_WPS")) {
+    const int v = atoi(e);
+    if (v < 1 || v > 4096) return fail(ctx, MICSA_ERR_ARG, "MICSA_REFRESH_WPS=%s", e);
+    wps = v;
+  }
 
   /* pinned staging for the start records; the previous upload from it must
    * have completed before it is rewritten */

@@ -143,6 +143,14 @@ __device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane) {
 
 /* --------------------------------------------------------------- sweeps */
 
+/* Programmatic dependent launch: let the next grid in the stream be
+ * scheduled now, then wait until the previous grid has completed and its
+ * memory operations are visible (a no-op for a plain launch). */
+__device__ __forceinline__ void grid_dependency_sync() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 /* Microcanonical update with demon D = D0 + 2*D1 and unsatisfied-bond
  * counts (j1 + 2*j2) + (j3 + 2*j4): the ISI boolean algebra of the
  * reference (main.cu:1037-1074).  Equivalent to: accept iff
@@ -306,6 +314,7 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
         const int *__restrict__ walk, const uint32_t *__restrict__ rnd,
         const __grid_constant__ micsa_tma tm) {
   constexpr int N = 2 * VW; /* words per pair */
+  grid_dependency_sync();
   using PR = pairs<VW, WIDE>;
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
   const uint32_t by = blockIdx.y;
@@ -565,6 +574,7 @@ k_sweep_async(const micsa_geo g, const int p, const int ic, const int ytiles, co
               uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
               const int *__restrict__ walk) {
   constexpr int VW = 2, N = 4;
+  grid_dependency_sync();
   const uint32_t L = g.L, Lh = g.Lh, W = g.W; /* W == 2 */
   const uint32_t by = blockIdx.y;
   const uint32_t tile = by % ytiles, s = by / ytiles;
@@ -712,6 +722,168 @@ k_sweep_async(const micsa_geo g, const int p, const int ic, const int ytiles, co
   }
 }
 
+/* ------------------------------------- sweep with register-pipelined loads */
+/* Operands of one z step of a thread's pair (k_sweep's loads). */
+template <int VW> struct step_ops {
+  uint32_t own[2 * VW], up[2 * VW], vn[2 * VW], vs[2 * VW], a0[2 * VW], a1[2 * VW], ext[VW];
+  uint32_t jb2;
+};
+
+/* The micSA half-sweep of k_sweep with the loads of z step t+1 issued before
+ * the arithmetic and stores of step t, so that a thread always has one step
+ * of loads in flight while it computes.  Issuing them early is safe: a
+ * thread's own spins and demon words are written only by that thread, and
+ * the other colour and the couplings are read-only during a half-sweep. */
+template <int VW, bool WIDE, int MINB>
+__global__ void __launch_bounds__(TPB, MINB)
+k_sweep_pipe(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
+             const int zc, const int pd, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
+             uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
+             const int *__restrict__ walk) {
+  constexpr int N = 2 * VW;
+  using PR = pairs<VW, WIDE>;
+  grid_dependency_sync();
+  const uint32_t L = g.L, Lh = g.Lh, W = g.W;
+  const uint32_t by = blockIdx.y;
+  const uint32_t tile = by % ytiles, sg = by / ytiles;
+  const uint32_t s = sg / G, grp = sg % G;
+  if (micsa_frozen(g, (int)s)) return;
+  const uint32_t y = tile * blockDim.y + threadIdx.y;
+  if (y >= L) return;
+  const uint32_t xa = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const uint32_t plane = L * Lh;
+  const uint32_t z0 = blockIdx.z * zc;
+  const uint32_t row = y * Lh + xa;
+  const uint32_t rowN = (y + 1 == L) ? xa : row + Lh;
+  const uint32_t rowS = (y == 0) ? row + (L - 1) * Lh : row - Lh;
+  const uint32_t rowXp = (xa + 2 == Lh) ? row + 2 - Lh : row + 2;
+  const uint32_t rowXm = (xa == 0) ? row + Lh - 1 : row - 1;
+  const size_t P = (size_t)g.P;
+  uint32_t *mine = spin + (size_t)(s * 2 + p) * P * W + grp * VW;
+  const uint32_t *oth = spin + (size_t)(s * 2 + (p ^ 1)) * P * W + grp * VW;
+  const uint8_t *jbp = jb + (size_t)(s * 2 + p) * P;
+  const uint64_t keep = l2_keep(), strm = l2_stream();
+
+  uint32_t drowA = row, drowB = row + 1, zd = z0;
+  bool dpair = true;
+  {
+    const int k = __ldg(walk + s);
+    const int sh = ((p == 0) == (ic < 3)) ? k : -k;
+    const int axis = ic < 3 ? ic : ic - 3;
+    if (axis == 0) {
+      int xd = (int)xa - sh;
+      xd += xd < 0 ? (int)Lh : (xd >= (int)Lh ? -(int)Lh : 0);
+      const int xe = (xd + 1 == (int)Lh) ? 0 : xd + 1;
+      drowA = y * Lh + (uint32_t)xd;
+      drowB = y * Lh + (uint32_t)xe;
+      dpair = !(sh & 1);
+    } else if (axis == 1) {
+      int yd = (int)y - 2 * sh;
+      yd += yd < 0 ? (int)L : (yd >= (int)L ? -(int)L : 0);
+      drowA = (uint32_t)yd * Lh + xa;
+      drowB = drowA + 1;
+    } else {
+      int t = (int)z0 - 2 * sh;
+      t += t < 0 ? (int)L : (t >= (int)L ? -(int)L : 0);
+      zd = (uint32_t)t;
+    }
+  }
+  const size_t dbase = ((size_t)(s * 2 + p) * g.nc + ic) * P * W + grp * VW;
+  uint32_t *q0b = d0 + dbase, *q1b = d1 + dbase;
+
+  auto load = [&](uint32_t t, step_ops<VW> &o) {
+    const uint32_t z = z0 + t, zo = z * plane, rowoff = (y + z + p) & 1;
+    uint32_t zt = zd + t;
+    zt -= zt >= L ? L : 0;
+    PR::ld(mine + (zo + row) * W, W, o.own, keep);
+    PR::ld_nc(oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, W, o.up, keep);
+    PR::ld_nc(oth + (zo + rowN) * W, W, o.vn, keep);
+    PR::ld_nc(oth + (zo + rowS) * W, W, o.vs, keep);
+    hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, o.ext, keep);
+    o.jb2 = ld_u16_keep(jbp + zo + row, keep);
+    const uint32_t sa = (zt * plane + drowA) * W;
+    if (dpair) {
+      PR::ld_na(q0b + sa, W, o.a0, strm);
+      PR::ld_na(q1b + sa, W, o.a1, strm);
+    } else {
+      const uint32_t sb = (zt * plane + drowB) * W;
+      uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
+      hint<VW>::ld_na(q0b + sa, x0, strm);
+      hint<VW>::ld_na(q0b + sb, x1, strm);
+      hint<VW>::ld_na(q1b + sa, y0, strm);
+      hint<VW>::ld_na(q1b + sb, y1, strm);
+#pragma unroll
+      for (int w = 0; w < VW; w++) {
+        o.a0[w] = x0[w]; o.a0[VW + w] = x1[w];
+        o.a1[w] = y0[w]; o.a1[VW + w] = y1[w];
+      }
+    }
+  };
+
+  uint32_t vm[N], v0[N];
+  PR::ld_nc(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, W, vm, keep);
+  PR::ld_nc(oth + (z0 * plane + row) * W, W, v0, keep);
+  step_ops<VW> cur;
+  load(0, cur);
+  uint32_t zdd = zd;
+#pragma unroll 2
+  for (uint32_t t = 0; t < (uint32_t)zc; t++) {
+    step_ops<VW> nxt;
+    if (t + 1 < (uint32_t)zc) load(t + 1, nxt);
+    if (pd > 0 && t + (uint32_t)pd < (uint32_t)zc) {
+      uint32_t zf = zdd + (uint32_t)pd;
+      if (zf >= L) zf -= L;
+      prefetch_l2(q0b + (zf * plane + drowA) * W);
+      prefetch_l2(q1b + (zf * plane + drowA) * W);
+    }
+    const uint32_t z = z0 + t, zo = z * plane, rowoff = (y + z + p) & 1;
+#pragma unroll
+    for (int site = 0; site < 2; site++) {
+      const uint32_t jb6 = (cur.jb2 >> (8 * site)) & 0xffu;
+      const uint32_t mE = jmask(jb6, 0), mN = jmask(jb6, 1), mU = jmask(jb6, 2);
+      const uint32_t mO = jmask(jb6, 3), mS = jmask(jb6, 4), mD = jmask(jb6, 5);
+#pragma unroll
+      for (int w = 0; w < VW; w++) {
+        const int o = site * VW + w;
+        const uint32_t cA = v0[w], cB = v0[VW + w], ex = cur.ext[w];
+        const uint32_t nE = site == 0 ? (rowoff ? cB : cA) : (rowoff ? ex : cB);
+        const uint32_t nO = site == 0 ? (rowoff ? cA : ex) : (rowoff ? cB : cA);
+        const uint32_t sw = cur.own[o];
+        const uint32_t f0 = sw ^ nE ^ mE, f1 = sw ^ cur.vn[o] ^ mN, f2 = sw ^ cur.up[o] ^ mU;
+        const uint32_t f3 = sw ^ nO ^ mO, f4 = sw ^ cur.vs[o] ^ mS, f5 = sw ^ vm[o] ^ mD;
+        const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
+        const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+        cur.own[o] = sw ^ isi_update(j1, j2, j3, j4, cur.a0[o], cur.a1[o]);
+      }
+    }
+    PR::st(mine + (zo + row) * W, W, cur.own, keep);
+    const uint32_t sa = (zdd * plane + drowA) * W;
+    if (dpair) {
+      PR::st(q0b + sa, W, cur.a0, strm);
+      PR::st(q1b + sa, W, cur.a1, strm);
+    } else {
+      const uint32_t sb = (zdd * plane + drowB) * W;
+      uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
+#pragma unroll
+      for (int w = 0; w < VW; w++) {
+        x0[w] = cur.a0[w]; x1[w] = cur.a0[VW + w];
+        y0[w] = cur.a1[w]; y1[w] = cur.a1[VW + w];
+      }
+      hint<VW>::st(q0b + sa, x0, strm);
+      hint<VW>::st(q0b + sb, x1, strm);
+      hint<VW>::st(q1b + sa, y0, strm);
+      hint<VW>::st(q1b + sb, y1, strm);
+    }
+#pragma unroll
+    for (int w = 0; w < N; w++) {
+      vm[w] = v0[w];
+      v0[w] = cur.up[w];
+    }
+    zdd = (zdd + 1 == L) ? 0 : zdd + 1;
+    cur = nxt;
+  }
+}
+
 /* ------------------------------------------------------ Philox + LUT bits */
 
 /* Philox4x32-10 (Salmon et al., SC'11): 10 rounds, Weyl key schedule. */
@@ -840,6 +1012,45 @@ k_from_ref(const micsa_geo g, const int p, const int ic, const int k,
     const site_xyz a = ref_site(g, p, h, lane), b = ref_site(g, p, h, lane + 32);
     dst[demon_slot(g, p, ic, k, a.x, a.y, a.z) * g.W + w] = lo;
     dst[demon_slot(g, p, ic, k, b.x, b.y, b.z) * g.W + w] = hi;
+  }
+}
+
+/* Coupling words of one sample, J[(p*6 + d)*H + h] as CopyDataOnDevice
+ * gathers them (main.cu:436-455), -> one bond byte per site (bit d = bond
+ * in direction d).  The backward words of blocks on the lattice's low edge
+ * along an axis are realigned first, by the block-edge rotation toward -x,
+ * -y, -z that d_oneMCstepBN applies to them (RotateO/S/D, main.cu:732-742,
+ * 910-927): the bit of block b receives the bit of block b-1 along the axis.
+ * Thread per (p, h, bit). */
+__device__ __forceinline__ uint64_t rot_back_word(int d, uint64_t v) {
+  if (d == 3) { const uint64_t m = 0x8888888888888888ULL; return ((v & m) >> 3) | ((v & ~m) << 1); }
+  if (d == 4) { const uint64_t m = 0xF000F000F000F000ULL; return ((v & m) >> 12) | ((v & ~m) << 4); }
+  const uint64_t m = 0xFFFF000000000000ULL;
+  return ((v & m) >> 48) | ((v & ~m) << 16);
+}
+
+__global__ void __launch_bounds__(TPB)
+k_couplings_from_ref(const micsa_geo g, const uint64_t *__restrict__ J, uint8_t *__restrict__ jb) {
+  const int64_t n = 2 * g.H * 64;
+  const int m = g.L >> 2, mh = m >> 1;
+  for (int64_t i = (int64_t)blockIdx.x * TPB + threadIdx.x; i < n; i += (int64_t)gridDim.x * TPB) {
+    const int bit = (int)(i & 63);
+    const int64_t ph = i >> 6;
+    const int p = (int)(ph / g.H);
+    const int64_t h = ph - (int64_t)p * g.H;
+    const int64_t q = h / mh;
+    const int bb = (int)(q % m), c = (int)(q / m);
+    const int a = 2 * (int)(h % mh) + ((bb + c + p) & 1);
+    const int edge[3] = {a == 0, bb == 0, c == 0};
+    uint32_t v = 0;
+#pragma unroll
+    for (int d = 0; d < 6; d++) {
+      uint64_t w = J[((int64_t)p * 6 + d) * g.H + h];
+      if (d >= 3 && edge[d - 3]) w = rot_back_word(d, w);
+      v |= (uint32_t)((w >> bit) & 1) << d;
+    }
+    const site_xyz s = ref_site(g, p, h, bit);
+    jb[(int64_t)p * g.P + ((int64_t)s.z * g.L + s.y) * g.Lh + (s.x >> 1)] = (uint8_t)v;
   }
 }
 
@@ -992,6 +1203,27 @@ k_overlap(const micsa_geo g, const uint32_t *__restrict__ spin, unsigned long lo
   }
 }
 
+/* Sweep launches with programmatic dependent launch (g.pdl): the next
+ * half-sweep's blocks are scheduled while this one drains and wait in
+ * griddepcontrol.wait (the kernels' first statement after the trigger) until
+ * it has completed and its writes are visible -- the same ordering as a plain
+ * launch, without the launch gap between the two grids. */
+template <typename... KArgs, typename... Args>
+cudaError_t launch_sweep(const micsa_geo &g, void (*k)(KArgs...), dim3 grid, dim3 block,
+                         size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t c = {};
+  c.gridDim = grid;
+  c.blockDim = block;
+  c.dynamicSmemBytes = smem;
+  c.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = g.pdl ? 1 : 0;
+  c.attrs = at;
+  c.numAttrs = 1;
+  return cudaLaunchKernelEx(&c, k, args...);
+}
+
 inline int blocks_for(int64_t n, int per_block) {
   int64_t b = (n + per_block - 1) / per_block;
   if (b < 1) b = 1;
@@ -1038,13 +1270,29 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
     if (g.occ == 4) {
       if ((e = cudaFuncSetAttribute(k_sweep_async<B1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)sb)) != cudaSuccess) return e;
-      k_sweep_async<B1><<<grid, block, sb, st>>>(g, p, ic, ytiles, zc, spin, d0, d1, jb, walk);
+      if ((e = launch_sweep(g, k_sweep_async<B1>, grid, block, sb, st, g, p, ic, ytiles, zc, spin, d0,
+                            d1, jb, walk)) != cudaSuccess) return e;
     } else {
       if ((e = cudaFuncSetAttribute(k_sweep_async<B0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)sb)) != cudaSuccess) return e;
-      k_sweep_async<B0><<<grid, block, sb, st>>>(g, p, ic, ytiles, zc, spin, d0, d1, jb, walk);
+      if ((e = launch_sweep(g, k_sweep_async<B0>, grid, block, sb, st, g, p, ic, ytiles, zc, spin, d0,
+                            d1, jb, walk)) != cudaSuccess) return e;
     }
     return cudaGetLastError();
+  }
+  if (micsa && g.pipe && !tma) {
+    /* register budgets: 2 blocks per SM (128 registers; always for 4-word
+     * vectors) or 3 (85) */
+    const bool b2 = g.occ == 2 || VW == 4;
+    if (G == 1)
+      return b2 ? launch_sweep(g, k_sweep_pipe<VW, true, 2>, grid, block, 0, st, g, p, ic, ytiles, G,
+                               zc, g.pd, spin, d0, d1, jb, walk)
+                : launch_sweep(g, k_sweep_pipe<VW, true, 3>, grid, block, 0, st, g, p, ic, ytiles, G,
+                               zc, g.pd, spin, d0, d1, jb, walk);
+    return b2 ? launch_sweep(g, k_sweep_pipe<VW, false, 2>, grid, block, 0, st, g, p, ic, ytiles, G, zc,
+                             g.pd, spin, d0, d1, jb, walk)
+              : launch_sweep(g, k_sweep_pipe<VW, false, 3>, grid, block, 0, st, g, p, ic, ytiles, G, zc,
+                             g.pd, spin, d0, d1, jb, walk);
   }
   micsa_tma none;
   const micsa_tma &t = tm ? *tm : none;
@@ -1056,8 +1304,9 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
                                                   (int)smem);                                     \
       if (e_ != cudaSuccess) return e_;                                                           \
     }                                                                                             \
-    k_sweep<VW, M, WD, B, T><<<grid, block, smem, st>>>(g, p, ic, ytiles, G, zc, g.pd, spin, d0,  \
-                                                        d1, jb, walk, rnd, t);                   \
+    const cudaError_t l_ = launch_sweep(g, k_sweep<VW, M, WD, B, T>, grid, block, smem, st, g, p, \
+                                        ic, ytiles, G, zc, g.pd, spin, d0, d1, jb, walk, rnd, t);  \
+    if (l_ != cudaSuccess) return l_;                                                             \
   } while (0)
   if (G == 1) {
     if (micsa) {
@@ -1151,6 +1400,12 @@ cudaError_t micsa_launch_walk_advance(const micsa_geo &g, int *walk, cudaStream_
 cudaError_t micsa_launch_from_ref(const micsa_geo &g, int p, int ic, int k, const uint64_t *ref,
                                   uint32_t *dst, cudaStream_t st) {
   k_from_ref<<<blocks_for(g.H * g.W, TPB / 32), TPB, 0, st>>>(g, p, ic, k, ref, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t micsa_launch_couplings_from_ref(const micsa_geo &g, const uint64_t *J, uint8_t *jb,
+                                            cudaStream_t st) {
+  k_couplings_from_ref<<<blocks_for(2 * g.H * 64, TPB), TPB, 0, st>>>(g, J, jb);
   return cudaGetLastError();
 }
 

@@ -28,9 +28,12 @@ struct micsa_geo {
   int64_t H;  /* reference words per colour, (L/4)^3/2 */
   int zc;     /* z planes per thread in the sweeps (divides L; 0 = default) */
   int pd;     /* L2 prefetch distance of the demon stream, in z steps (0 = off) */
-  int occ;    /* sweep variant: 4 = register cap for 4 blocks per SM, else the compiler's */
+  int occ;    /* sweep register budget in blocks per SM: 4 = cap for 4 blocks, 3 = the
+                 default (the pipelined variant: 3 or 2) */
   int tma;    /* 1: the sweep stages its demon tiles in shared memory by TMA */
   int async;  /* 1: the sweep double-buffers each step's operands with cp.async (W = 2) */
+  int pipe;   /* 1: the sweep loads each z step's operands into registers one step ahead */
+  int pdl;    /* 1: sweeps launched with programmatic dependent launch */
   int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */
@@ -86,6 +89,10 @@ cudaError_t micsa_launch_walk_advance(const micsa_geo &g, int *walk,
 cudaError_t micsa_launch_from_ref(const micsa_geo &g, int p, int ic, int k,
                                   const uint64_t *ref, uint32_t *dst,
                                   cudaStream_t st);
+/* reference coupling words J[(p*6 + d)*H + h] of one sample (device) ->
+ * that sample's bond bytes jb[2][P] */
+cudaError_t micsa_launch_couplings_from_ref(const micsa_geo &g, const uint64_t *J, uint8_t *jb,
+                                            cudaStream_t st);
 cudaError_t micsa_launch_to_ref(const micsa_geo &g, int p, int ic,
                                 const int *walk, int sample,
                                 const uint32_t *src, uint64_t *ref,

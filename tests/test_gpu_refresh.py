@@ -56,6 +56,42 @@ def test_gpu_refresh_equals_host_draw_twice(L, nr, nc, ns):
             assert bytes(prc) == bytes(hp) and bytes(xo) == bytes(hx), rnd
 
 
+@pytest.mark.parametrize("order", [(2, 1, 0), (1, 0, 2), (0, 0, 1)])
+def test_gpu_refresh_thresholds_in_any_order(order):
+    """The kernel counts the thresholds above each draw as InitWalkers does,
+    so thresholds that are not ascending (no beta gives them) still give
+    InitWalkers' demons."""
+    L, nr, nc, ns = 16, 64, 2, 2
+    t = micsa.thresholds(BETA)
+    thr = np.array([t[i] for i in order], dtype=np.uint64)
+    prc, xo = _streams(ns * nr, 2024)
+    hp, hx = _copy(prc, micsa.PRC), _copy(xo, micsa.Xoshiro)
+    with micsa.Context(L, nr, ns, nc) as ctx:
+        ctx.refresh_demons(0, prc, xo, thr)
+        for s in range(ns):
+            w0, w1 = _host_draw(L, nr, nc, hp, hx, s, thr)
+            g0, g1 = ctx.download_demons(s)
+            assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
+    assert bytes(prc) == bytes(hp) and bytes(xo) == bytes(hx)
+
+
+@pytest.mark.parametrize("wps", ["3", "128"])
+def test_gpu_refresh_segment_lengths(monkeypatch, wps):
+    """Pinned segment lengths (MICSA_REFRESH_WPS) change only the launch."""
+    monkeypatch.setenv("MICSA_REFRESH_WPS", wps)
+    L, nr, nc, ns = 32, 64, 3, 1
+    thr = micsa.thresholds(BETA)
+    prc, xo = _streams(ns * nr, 555)
+    hp, hx = _copy(prc, micsa.PRC), _copy(xo, micsa.Xoshiro)
+    with micsa.Context(L, nr, ns, nc) as ctx:
+        for rnd in range(2):
+            ctx.refresh_demons(0, prc, xo, thr)
+            w0, w1 = _host_draw(L, nr, nc, hp, hx, 0, thr)
+            g0, g1 = ctx.download_demons(0)
+            assert np.array_equal(g0, w0) and np.array_equal(g1, w1), rnd
+            assert bytes(prc) == bytes(hp) and bytes(xo) == bytes(hx), rnd
+
+
 def test_gpu_refresh_part_of_the_samples_after_walks():
     """A refresh of samples [1, 3) resets their walk and leaves sample 0."""
     L, nr, nc, ns = 16, 32, 6, 3

@@ -90,3 +90,38 @@ def test_async_staged_sweep_matches_oracle(L, nc, ns, split, occ):
             g0, g1 = ctx.download_demons(s)
             assert np.array_equal(ge, e) and np.array_equal(go, o), s
             assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
+
+
+@pytest.mark.parametrize("L,nr,nc,ns,split,occ,zc,pd", [(32, 64, 6, 2, 0, 3, 4, 2), (40, 32, 3, 1, 0, 2, 8, 0),
+                                                       (64, 128, 6, 2, 1, 3, 8, 4),
+                                                       (96, 64, 5, 2, 1, 2, 16, 2),
+                                                       (48, 96, 2, 3, 0, 3, 1, 0)])
+def test_pipelined_sweep_matches_oracle(L, nr, nc, ns, split, occ, zc, pd):
+    """The sweep with each z step's loads issued one step ahead, pinned on,
+    against the oracle over every walk shift (32, 64, 96 and 128 replicas:
+    one, two, three-of-one and four-word vectors)."""
+    old = _pinned({"MICSA_SWEEP_ZC": str(zc), "MICSA_SWEEP_PD": str(pd), "MICSA_SWEEP_PIPE": "1",
+                   "MICSA_SWEEP_SPLIT": str(split), "MICSA_SWEEP_OCC": str(occ),
+                   "MICSA_RESIDENT": "0"})
+    try:
+        ctx = micsa.Context(L, nr, ns, nc)
+        assert "load=pipe" in ctx.tuning(), ctx.tuning()
+    finally:
+        _restore(old)
+    rng = np.random.default_rng(11 * L + ns)
+    st = random_state(rng, L, nr, nc, ns)
+    iters = L // 2 + 3
+    with ctx:
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            ctx.upload_couplings(s, J)
+            ctx.upload_spins(s, e, o)
+            ctx.upload_demons(s, w0, w1)
+        ctx.iterate(iters)
+        ctx.synchronize()
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            for _ in range(iters):
+                oracle.micsa_iteration(L, nr, nc, J, e, o, w0, w1, 8)
+            ge, go = ctx.download_spins(s)
+            g0, g1 = ctx.download_demons(s)
+            assert np.array_equal(ge, e) and np.array_equal(go, o), s
+            assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
