@@ -160,13 +160,15 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
  * launch for all samples, 1: sample-major, one launch per sample>
  * occ=<blocks per SM the registers are allocated for> load=<direct | tma:
  * demon tiles staged by TMA | async: operands double-buffered by cp.async |
- * pipe: each z step's loads issued one step ahead into registers> |
- * <zc>/<pd>/<split>/<occ>/<load 0|1|2|3>:<ms per half-sweep> ...", with
+ * pipe: each z step's loads issued one step ahead into registers>
+ * tile=<default | row: blocks span whole rows along x> |
+ * <zc>/<pd>/<split>/<occ>/<load 0|1|2|3>/<tile 0|1>:<ms per half-sweep> ...", with
  * " cached" before the "|" when the choice and its table were taken over
  * from an earlier context of the same device, L, nr, samples and nc in this
  * process (MICSA_TUNE_CACHE=0 times every context instead).  The
  * environment variables MICSA_SWEEP_ZC, MICSA_SWEEP_PD, MICSA_SWEEP_SPLIT,
- * MICSA_SWEEP_OCC, MICSA_SWEEP_TMA, MICSA_SWEEP_ASYNC and MICSA_SWEEP_PIPE, read by
+ * MICSA_SWEEP_OCC, MICSA_SWEEP_TMA, MICSA_SWEEP_ASYNC, MICSA_SWEEP_PIPE and
+ * MICSA_SWEEP_TILE (=row), read by
  * micsa_create, pin the shape and skip the timing (no candidates listed
  * then).  The reference has fixed launch geometry (calculate_blocks,
  * ini.c:580-602). */

@@ -23,7 +23,7 @@
 #include "micsa_jump.h"
 #include "micsa_kernels.cuh"
 
-#define MICSA_TUNE_MAX 160
+#define MICSA_TUNE_MAX 320
 
 struct micsa_ctx {
   micsa_config cfg;
@@ -50,7 +50,7 @@ struct micsa_ctx {
   int ntune = 0;           /* launch shapes timed at creation */
   int tune_zc[MICSA_TUNE_MAX] = {0}, tune_pd[MICSA_TUNE_MAX] = {0};
   int tune_split[MICSA_TUNE_MAX] = {0}, tune_occ[MICSA_TUNE_MAX] = {0};
-  int tune_tma[MICSA_TUNE_MAX] = {0};
+  int tune_tma[MICSA_TUNE_MAX] = {0}, tune_tw[MICSA_TUNE_MAX] = {0};
   double tune_ms[MICSA_TUNE_MAX] = {0};
   int tune_cached = 0; /* the shape came from an earlier context's timing */
   /* demon refresh on the device: jump tables of one segment length */
@@ -225,8 +225,8 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
  * choice and table instead of timing again, so batches and servers that open
  * many contexts of a few shapes pay for each shape once. */
 struct tune_entry {
-  int zc, pd, split, occ, tma, async, pipe, n;
-  std::vector<int> zcs, pds, splits, occs, tmas;
+  int zc, pd, split, occ, tma, async, pipe, tw, n;
+  std::vector<int> zcs, pds, splits, occs, tmas, tws;
   std::vector<double> ms;
 };
 std::mutex tune_mu;
@@ -237,10 +237,12 @@ std::tuple<int, int, int, int, int, int> tune_key(const micsa_ctx *ctx) {
                          ctx->tma.ok ? 1 : 0);
 }
 
-/* Launch-shape autotuner: time the half-sweeps of whole iterations, in their
- * real launch order, for every z-chunk length that divides L, prefetch
- * distance, sample order (merged or sample-major) and register budget, on the
- * freshly zeroed buffers; keep the fastest, then zero the buffers again.  Results do not
+/* Launch-shape autotuner: time whole iterations (the half-sweeps in their
+ * real launch order and the walk, replayed as a graph) for every z-chunk
+ * length that divides L, prefetch distance, sample order (merged or
+ * sample-major), register budget, load scheme and block shape, on the
+ * freshly zeroed buffers; keep the fastest, then zero the buffers and the
+ * walks again.  Results do not
  * depend on the choice (each site is updated by exactly one thread either
  * way); only the speed does.  MICSA_TUNE_CACHE=0 times every context afresh
  * instead of reusing the process's earlier choice for the same shape. */
@@ -264,11 +266,12 @@ int autotune(micsa_ctx *ctx) {
     g.pd = pd;
     const char *es = getenv("MICSA_SWEEP_SPLIT"), *eo = getenv("MICSA_SWEEP_OCC"),
                *et = getenv("MICSA_SWEEP_TMA"), *ea = getenv("MICSA_SWEEP_ASYNC"),
-               *ep2 = getenv("MICSA_SWEEP_PIPE");
+               *ep2 = getenv("MICSA_SWEEP_PIPE"), *ew = getenv("MICSA_SWEEP_TILE");
     ctx->split = es && atoi(es) && g.ns > 1;
     g.tma = et && atoi(et) && ctx->tma.ok;
     g.async = ea && atoi(ea) && g.W == 2 && !g.tma;
     g.pipe = ep2 && atoi(ep2) && !g.tma && !g.async;
+    g.tw = ew && !strcmp(ew, "row") && !g.tma && micsa_sweep_wide_differs(g.L);
     const int oc = eo ? atoi(eo) : 3;
     g.occ = g.pipe ? (oc == 2 ? 2 : 3) : (oc == 4 ? 4 : 3);
     ctx->ntune = 0;
@@ -288,6 +291,7 @@ int autotune(micsa_ctx *ctx) {
       g.tma = t.tma;
       g.async = t.async;
       g.pipe = t.pipe;
+      g.tw = t.tw;
       ctx->ntune = t.n;
       for (int c = 0; c < t.n; c++) {
         ctx->tune_zc[c] = t.zcs[c];
@@ -295,6 +299,7 @@ int autotune(micsa_ctx *ctx) {
         ctx->tune_split[c] = t.splits[c];
         ctx->tune_occ[c] = t.occs[c];
         ctx->tune_tma[c] = t.tmas[c];
+        ctx->tune_tw[c] = t.tws[c];
         ctx->tune_ms[c] = t.ms[c];
       }
       ctx->tune_cached = 1;
@@ -306,13 +311,15 @@ int autotune(micsa_ctx *ctx) {
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
   int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, best_tma = 0;
-  int best_async = 0, best_pipe = 0, n = 0;
+  int best_async = 0, best_pipe = 0, best_tw = 0, n = 0;
+  const int ntw = micsa_sweep_wide_differs(g.L) ? 2 : 1;
   const int reps = 3;
   const int nocc = g.W % 4 ? 2 : 1; /* the 4-blocks variant exists for VW <= 2 */
   /* tm: 0 direct loads, 1 TMA-staged demon tiles, 2 cp.async double buffer (W = 2),
    * 3 loads pipelined one step ahead in registers (register budget for 3 or 2
    * blocks per SM instead of 3 or 4) */
   for (int tm = 0; tm < 4; tm++)
+  for (int tw = 0; tw < ntw; tw++)
   for (int oc = 0; oc < nocc; oc++)
   for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
   for (int c = 0; c < nz; c++)
@@ -320,19 +327,24 @@ int autotune(micsa_ctx *ctx) {
       if (pds[d] && pds[d] >= zcs[c]) continue; /* prefetch only within a slab */
       if (tm == 1 && (!ctx->tma.ok || zcs[c] > 4)) continue; /* staged tiles: <= 4 planes */
       if (tm == 2 && (g.W != 2 || pds[d])) continue;          /* no L2 prefetch there */
+      if (tw && (tm == 1 || tm == 2)) continue; /* whole-row blocks: direct and pipelined loads */
       g.zc = zcs[c];
       g.pd = pds[d];
       g.occ = tm == 3 ? (oc ? 2 : 3) : (oc ? 4 : 3);
       g.tma = tm == 1;
       g.async = tm == 2;
       g.pipe = tm == 3;
+      g.tw = tw;
       /* one iteration's half-sweeps in their launch order, captured and
        * replayed as a graph the way micsa_iterate runs them: timed launch by
        * launch, small lattices would measure the host's launch rate */
       cudaGraph_t gr = nullptr;
       cudaGraphExec_t ge = nullptr;
       MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      const cudaError_t le = launch_halves(ctx, g, sp, 0, g.nc, nullptr);
+      cudaError_t le = launch_halves(ctx, g, sp, 0, g.nc, nullptr);
+      /* with the walk advancing, as in a run: the x translation of the demon
+       * planes misaligns their rows at most shifts, never at shift 0 */
+      if (le == cudaSuccess) le = micsa_launch_walk_advance(g, ctx->walk, ctx->stream);
       const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &gr);
       MICSA_CK(le);
       MICSA_CK(ce);
@@ -355,6 +367,7 @@ int autotune(micsa_ctx *ctx) {
         ctx->tune_split[n] = sp;
         ctx->tune_occ[n] = g.occ;
         ctx->tune_tma[n] = tm;
+        ctx->tune_tw[n] = tw;
         ctx->tune_ms[n] = per;
         n++;
       }
@@ -367,6 +380,7 @@ int autotune(micsa_ctx *ctx) {
         best_tma = g.tma;
         best_async = g.async;
         best_pipe = g.pipe;
+        best_tw = g.tw;
       }
     }
   ctx->ntune = n;
@@ -377,6 +391,7 @@ int autotune(micsa_ctx *ctx) {
   g.tma = best_tma;
   g.async = best_async;
   g.pipe = best_pipe;
+  g.tw = best_tw;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (use_cache) {
@@ -388,12 +403,14 @@ int autotune(micsa_ctx *ctx) {
     t.tma = g.tma;
     t.async = g.async;
     t.pipe = g.pipe;
+    t.tw = g.tw;
     t.n = n;
     t.zcs.assign(ctx->tune_zc, ctx->tune_zc + n);
     t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
     t.splits.assign(ctx->tune_split, ctx->tune_split + n);
     t.occs.assign(ctx->tune_occ, ctx->tune_occ + n);
     t.tmas.assign(ctx->tune_tma, ctx->tune_tma + n);
+    t.tws.assign(ctx->tune_tw, ctx->tune_tw + n);
     t.ms.assign(ctx->tune_ms, ctx->tune_ms + n);
     std::lock_guard<std::mutex> lk(tune_mu);
     tune_cache.emplace(tune_key(ctx), std::move(t)); /* the first timing of a shape stays */
@@ -449,6 +466,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.tma = 0;
   g.async = 0;
   g.pipe = 0;
+  g.tw = 0;
   {
     /* MICSA_PDL=0: plain launches of the sweeps */
     const char *e = getenv("MICSA_PDL");
@@ -518,6 +536,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->spin, 0, 4 * s.spin_w, ctx->stream));
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem0, 0, 4 * s.dem_w, ctx->stream));
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->dem1, 0, 4 * s.dem_w, ctx->stream));
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->walk, 0, sizeof(int) * MICSA_MAX_SAMPLES, ctx->stream));
   MICSA_CK_CREATE(cudaStreamSynchronize(ctx->stream));
 #undef MICSA_CK_CREATE
   return MICSA_OK;
@@ -525,14 +544,14 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s%s |", ctx->g.zc, ctx->g.pd,
-                   ctx->split, ctx->g.occ,
+  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s%s |", ctx->g.zc,
+                   ctx->g.pd, ctx->split, ctx->g.occ,
                    ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : "direct")),
-                   ctx->tune_cached ? " cached" : "");
+                   ctx->g.tw ? "row" : "default", ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
-    k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],
+    k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],
                   ctx->tune_pd[c], ctx->tune_split[c], ctx->tune_occ[c], ctx->tune_tma[c],
-                  ctx->tune_ms[c]);
+                  ctx->tune_tw[c], ctx->tune_ms[c]);
   return MICSA_OK;
 }
 

@@ -122,9 +122,23 @@ __device__ __forceinline__ int64_t demon_slot(const micsa_geo &g, int p, int ic,
   return ((int64_t)z * L + y) * g.Lh + (x >> 1);
 }
 
+/* all-ones if bond bit d of the site's coupling byte is set (one signed
+ * bit-field extract) */
 __device__ __forceinline__ uint32_t jmask(uint32_t jb, int d) {
-  return 0u - ((jb >> d) & 1u);
+  uint32_t r;
+  asm("bfe.s32 %0, %1, %2, 1;" : "=r"(r) : "r"(jb), "r"(d));
+  return r;
 }
+
+/* three-input bitwise function by truth table (a = 0xF0, b = 0xCC, c = 0xAA) */
+template <int LUT>
+__device__ __forceinline__ uint32_t lop3(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("lop3.b32 %0, %1, %2, %3, %4;" : "=r"(d) : "r"(a), "r"(b), "r"(c), "n"(LUT));
+  return d;
+}
+__device__ __forceinline__ uint32_t xor3(uint32_t a, uint32_t b, uint32_t c) { return lop3<0x96>(a, b, c); }
+__device__ __forceinline__ uint32_t maj3(uint32_t a, uint32_t b, uint32_t c) { return lop3<0xe8>(a, b, c); }
 
 /* 32x32 bit transpose across a warp: lane c returns the word whose bit i is
  * bit c of lane i's input. */
@@ -152,20 +166,21 @@ __device__ __forceinline__ void grid_dependency_sync() {
 }
 
 /* Microcanonical update with demon D = D0 + 2*D1 and unsatisfied-bond
- * counts (j1 + 2*j2) + (j3 + 2*j4): the ISI boolean algebra of the
- * reference (main.cu:1037-1074).  Equivalent to: accept iff
- * 0 <= D + u - 3 <= 3, then D <- D + u - 3. */
+ * counts (j1 + 2*j2) + (j3 + 2*j4): accept iff 0 <= D + u - 3 <= 3, then
+ * D <- D + u - 3 -- the function the reference's ISI boolean algebra
+ * computes (main.cu:1037-1074), equal to it on all 64 inputs, in a
+ * shorter circuit: T = D + u summed carry-save into bits s0 + 2 s1 + 4 s2
+ * + 8 c3; accepted iff 3 <= T <= 6, i.e. !c3 and s2 ^ (s1 & s0); then
+ * D0 = !s0 and D1 = s2 & (s0 | s1). */
 __device__ __forceinline__ uint32_t isi_update(uint32_t j1, uint32_t j2, uint32_t j3,
                                                uint32_t j4, uint32_t &D0, uint32_t &D1) {
-  const uint32_t x13 = j1 ^ j3, x24 = j2 ^ j4;
-  const uint32_t sub = (x24 & ~j1 & ~j3) | (~j2 & ~j4);
-  const uint32_t s0 = ~x13;
-  uint32_t s1 = ~x24 & (x13 | (s0 & ~(j1 ^ j2)));
-  s1 = (~sub & s1) | (sub & (s1 ^ s0));
-  const uint32_t n0 = D0 ^ s0, k1 = D0 & s0, k2 = D1 ^ s1, n1 = k1 ^ k2, k3 = D1 & s1;
-  const uint32_t flip = ~((k3 | (k2 & k1)) ^ sub);
-  D0 = (flip & n0) | (~flip & D0);
-  D1 = (flip & n1) | (~flip & D1);
+  const uint32_t s0 = xor3(D0, j1, j3), c0 = maj3(D0, j1, j3);
+  const uint32_t t = xor3(D1, j2, j4), cc = maj3(D1, j2, j4);
+  const uint32_t s1 = t ^ c0, s2 = lop3<0x78>(cc, t, c0), c3 = lop3<0x80>(cc, t, c0);
+  const uint32_t flip = lop3<0x78>(s2, s1, s0) & ~c3;
+  const uint32_t d1 = lop3<0xe0>(s2, s0, s1);
+  D0 = lop3<0x3a>(flip, s0, D0); /* flip ? !s0 : D0 */
+  D1 = lop3<0xca>(flip, d1, D1); /* flip ? d1 : D1 */
   return flip;
 }
 
@@ -320,6 +335,8 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
   const uint32_t by = blockIdx.y;
   const uint32_t tile = by % ytiles, sg = by / ytiles; /* block-uniform */
   const uint32_t s = sg / G, grp = sg % G;
+  /* the walk and the run flag are loaded together: one round trip */
+  const int kwalk = MICSA ? __ldg(walk + s) : 0;
   if (micsa_frozen(g, (int)s)) return;
   const uint32_t y = tile * blockDim.y + threadIdx.y;
   if (y >= L) return;
@@ -344,7 +361,7 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
   uint32_t drowA = row, drowB = row + 1, zd = z0;
   bool dpair = true;
   if (MICSA) {
-    const int k = __ldg(walk + s);
+    const int k = kwalk;
     const int sh = ((p == 0) == (ic < 3)) ? k : -k; /* in units of 2 sites */
     const int axis = ic < 3 ? ic : ic - 3;
     if (axis == 0) {
@@ -380,7 +397,7 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
   int off = 0;
   bool staged = false;
   if (TMA && MICSA) {
-    const int k = __ldg(walk + s);
+    const int k = kwalk;
     const int sh = ((p == 0) == (ic < 3)) ? k : -k;
     const int axis = ic < 3 ? ic : ic - 3;
     const int xb = 2 * blockIdx.x * blockDim.x, yb = tile * blockDim.y;
@@ -497,10 +514,10 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
         const uint32_t nE = site == 0 ? (rowoff ? cB : cA) : (rowoff ? ex : cB);
         const uint32_t nO = site == 0 ? (rowoff ? cA : ex) : (rowoff ? cB : cA);
         const uint32_t sw = own[o];
-        const uint32_t f0 = sw ^ nE ^ mE, f1 = sw ^ vn[o] ^ mN, f2 = sw ^ up[o] ^ mU;
-        const uint32_t f3 = sw ^ nO ^ mO, f4 = sw ^ vs[o] ^ mS, f5 = sw ^ vm[o] ^ mD;
-        const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
-        const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+        const uint32_t f0 = xor3(sw, nE, mE), f1 = xor3(sw, vn[o], mN), f2 = xor3(sw, up[o], mU);
+        const uint32_t f3 = xor3(sw, nO, mO), f4 = xor3(sw, vs[o], mS), f5 = xor3(sw, vm[o], mD);
+        const uint32_t j1 = xor3(f0, f1, f2), j2 = maj3(f0, f1, f2);
+        const uint32_t j3 = xor3(f3, f4, f5), j4 = maj3(f3, f4, f5);
         uint32_t flip;
         if (MICSA)
           flip = isi_update(j1, j2, j3, j4, a0[o], a1[o]);
@@ -578,6 +595,8 @@ k_sweep_async(const micsa_geo g, const int p, const int ic, const int ytiles, co
   const uint32_t L = g.L, Lh = g.Lh, W = g.W; /* W == 2 */
   const uint32_t by = blockIdx.y;
   const uint32_t tile = by % ytiles, s = by / ytiles;
+  /* the walk and the run flag are loaded together: one round trip */
+  const int kwalk = __ldg(walk + s);
   if (micsa_frozen(g, (int)s)) return;
   const uint32_t y = tile * blockDim.y + threadIdx.y;
   if (y >= L) return;
@@ -598,7 +617,7 @@ k_sweep_async(const micsa_geo g, const int p, const int ic, const int ytiles, co
   uint32_t drowA = row, drowB = row + 1, zd = z0;
   bool dpair = true;
   {
-    const int k = __ldg(walk + s);
+    const int k = kwalk;
     const int sh = ((p == 0) == (ic < 3)) ? k : -k;
     const int axis = ic < 3 ? ic : ic - 3;
     if (axis == 0) {
@@ -692,10 +711,10 @@ k_sweep_async(const micsa_geo g, const int p, const int ic, const int ytiles, co
         const uint32_t nE = site == 0 ? (rowoff ? cB : cA) : (rowoff ? ex : cB);
         const uint32_t nO = site == 0 ? (rowoff ? cA : ex) : (rowoff ? cB : cA);
         const uint32_t sw = own[o];
-        const uint32_t f0 = sw ^ nE ^ mE, f1 = sw ^ vn[o] ^ mN, f2 = sw ^ up[o] ^ mU;
-        const uint32_t f3 = sw ^ nO ^ mO, f4 = sw ^ vs[o] ^ mS, f5 = sw ^ vm[o] ^ mD;
-        const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
-        const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+        const uint32_t f0 = xor3(sw, nE, mE), f1 = xor3(sw, vn[o], mN), f2 = xor3(sw, up[o], mU);
+        const uint32_t f3 = xor3(sw, nO, mO), f4 = xor3(sw, vs[o], mS), f5 = xor3(sw, vm[o], mD);
+        const uint32_t j1 = xor3(f0, f1, f2), j2 = maj3(f0, f1, f2);
+        const uint32_t j3 = xor3(f3, f4, f5), j4 = maj3(f3, f4, f5);
         own[o] = sw ^ isi_update(j1, j2, j3, j4, a0[o], a1[o]);
       }
     }
@@ -747,6 +766,8 @@ k_sweep_pipe(const micsa_geo g, const int p, const int ic, const int ytiles, con
   const uint32_t by = blockIdx.y;
   const uint32_t tile = by % ytiles, sg = by / ytiles;
   const uint32_t s = sg / G, grp = sg % G;
+  /* the walk and the run flag are loaded together: one round trip */
+  const int kwalk = __ldg(walk + s);
   if (micsa_frozen(g, (int)s)) return;
   const uint32_t y = tile * blockDim.y + threadIdx.y;
   if (y >= L) return;
@@ -767,7 +788,7 @@ k_sweep_pipe(const micsa_geo g, const int p, const int ic, const int ytiles, con
   uint32_t drowA = row, drowB = row + 1, zd = z0;
   bool dpair = true;
   {
-    const int k = __ldg(walk + s);
+    const int k = kwalk;
     const int sh = ((p == 0) == (ic < 3)) ? k : -k;
     const int axis = ic < 3 ? ic : ic - 3;
     if (axis == 0) {
@@ -849,10 +870,10 @@ k_sweep_pipe(const micsa_geo g, const int p, const int ic, const int ytiles, con
         const uint32_t nE = site == 0 ? (rowoff ? cB : cA) : (rowoff ? ex : cB);
         const uint32_t nO = site == 0 ? (rowoff ? cA : ex) : (rowoff ? cB : cA);
         const uint32_t sw = cur.own[o];
-        const uint32_t f0 = sw ^ nE ^ mE, f1 = sw ^ cur.vn[o] ^ mN, f2 = sw ^ cur.up[o] ^ mU;
-        const uint32_t f3 = sw ^ nO ^ mO, f4 = sw ^ cur.vs[o] ^ mS, f5 = sw ^ vm[o] ^ mD;
-        const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
-        const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+        const uint32_t f0 = xor3(sw, nE, mE), f1 = xor3(sw, cur.vn[o], mN), f2 = xor3(sw, cur.up[o], mU);
+        const uint32_t f3 = xor3(sw, nO, mO), f4 = xor3(sw, cur.vs[o], mS), f5 = xor3(sw, vm[o], mD);
+        const uint32_t j1 = xor3(f0, f1, f2), j2 = maj3(f0, f1, f2);
+        const uint32_t j3 = xor3(f3, f4, f5), j4 = maj3(f3, f4, f5);
         cur.own[o] = sw ^ isi_update(j1, j2, j3, j4, cur.a0[o], cur.a1[o]);
       }
     }
@@ -1237,9 +1258,15 @@ inline int blocks_for(int64_t n, int per_block) {
 
 /* tile of the sweep for this L: tx pairs along x/2 (the largest power of two
  * <= 32 dividing L/4, L/4 even) x ty rows, ty*tx = TPB threads */
-static void sweep_tile(int L, int *tx, int *ty) {
+/* Block shape of the sweeps: tx threads along x (two x/2 positions each) by
+ * ty rows.  Default: the largest power of two up to 32 dividing L/4.  Whole
+ * rows (wide, when L/4 is not already that and fits a block): a row's demon
+ * words are then read as one run, so the x translation of the demon walk
+ * shifts one run instead of misaligning several short ones. */
+static void sweep_tile(int L, int wide, int *tx, int *ty) {
   int x = 32;
   while ((L / 4) % x) x >>= 1;
+  if (wide && L / 4 <= TPB / 2) x = L / 4;
   *tx = x;
   *ty = TPB / x;
 }
@@ -1250,7 +1277,7 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
                             const uint32_t *rnd, const micsa_tma *tm, cudaStream_t st) {
   const int G = g.W / VW;
   int tx, ty;
-  sweep_tile(g.L, &tx, &ty);
+  sweep_tile(g.L, g.tw, &tx, &ty);
   const int ytiles = (g.L + ty - 1) / ty;
   /* z chunk per thread: long columns at large L, more threads at small L */
   const int zc = g.zc > 0 ? g.zc : ((g.L >= 128 && g.L % 16 == 0) ? 16 : (g.L >= 48 ? 8 : 2));
@@ -1340,7 +1367,7 @@ cudaError_t micsa_make_tma(const micsa_geo &g, const uint32_t *d0, const uint32_
     return cudaSuccess; /* no staged sweep; not an error */
   }
   int tx, ty;
-  sweep_tile(g.L, &tx, &ty);
+  sweep_tile(g.L, 0, &tx, &ty);
   const cuuint64_t row = (cuuint64_t)g.Lh * g.W; /* words per (plane, y) row */
   /* the tile plus 4 words (16 bytes) for a start rounded down, at most a row */
   int box_w = 2 * tx * g.W + 4;
@@ -1450,6 +1477,13 @@ cudaError_t micsa_launch_overlap(const micsa_geo &g, const uint32_t *spin, unsig
   dim3 grid(measure_blocks(2 * g.P, (int64_t)3 * nd * g.W * g.ns), 3 * nd, g.ns * g.W);
   k_overlap<<<grid, TPB, 0, st>>>(g, spin, qd, c4d);
   return cudaGetLastError();
+}
+
+int micsa_sweep_wide_differs(int L) {
+  int a, b, c, d;
+  sweep_tile(L, 0, &a, &b);
+  sweep_tile(L, 1, &c, &d);
+  return a != c;
 }
 
 int micsa_sweep_zc_candidates(int L, int *out, int max) {
@@ -1651,8 +1685,8 @@ k_resident(const micsa_geo g, const int n, uint32_t *__restrict__ spin,
           const uint32_t f3 = sw ^ oth[row + xo] ^ jmask(jb6, 3);
           const uint32_t f4 = sw ^ oth[(z * L + ym) * Lh + xh] ^ jmask(jb6, 4);
           const uint32_t f5 = sw ^ oth[(zm * L + y) * Lh + xh] ^ jmask(jb6, 5);
-          const uint32_t k1 = f0 ^ f1, j1 = k1 ^ f2, j2 = (f0 & f1) ^ (k1 & f2);
-          const uint32_t k4 = f3 ^ f4, j3 = k4 ^ f5, j4 = (f3 & f4) ^ (k4 & f5);
+          const uint32_t j1 = xor3(f0, f1, f2), j2 = maj3(f0, f1, f2);
+          const uint32_t j3 = xor3(f3, f4, f5), j4 = maj3(f3, f4, f5);
           int slot;
           if (axis == 0) slot = row + ((xh - sh) & (Lh - 1));
           else if (axis == 1) slot = (z * L + ((y - 2 * sh) & (L - 1))) * Lh + xh;

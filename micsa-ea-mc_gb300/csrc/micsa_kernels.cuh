@@ -34,6 +34,7 @@ struct micsa_geo {
   int async;  /* 1: the sweep double-buffers each step's operands with cp.async (W = 2) */
   int pipe;   /* 1: the sweep loads each z step's operands into registers one step ahead */
   int pdl;    /* 1: sweeps launched with programmatic dependent launch */
+  int tw;     /* 1: sweep blocks span whole rows along x (when that differs) */
   int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */
@@ -60,6 +61,9 @@ cudaError_t micsa_make_tma(const micsa_geo &g, const uint32_t *d0, const uint32_
 /* waits of the staged sweep that ran out since the process started (0 unless
  * a TMA copy never completed; the sweep then read the words directly) */
 cudaError_t micsa_tma_timeout_count(unsigned *n);
+
+/* 1 if whole-row sweep blocks (micsa_geo.tw) differ from the default shape at this L */
+int micsa_sweep_wide_differs(int L);
 
 /* slab depths the sweep can use for this L (divisors of L, ascending) */
 int micsa_sweep_zc_candidates(int L, int *out, int max);

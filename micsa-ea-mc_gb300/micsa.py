@@ -338,8 +338,8 @@ class Context:
 
     def tuning(self):
         """The autotuner's choice and timings, as a text line."""
-        buf = C.create_string_buffer(4096)
-        check(self.h, lib().micsa_tuning_report(self.h, buf, 4096), "tuning_report")
+        buf = C.create_string_buffer(16384)
+        check(self.h, lib().micsa_tuning_report(self.h, buf, 16384), "tuning_report")
         return buf.value.decode()
 
     def kernel_launches(self):

@@ -125,3 +125,36 @@ def test_pipelined_sweep_matches_oracle(L, nr, nc, ns, split, occ, zc, pd):
             g0, g1 = ctx.download_demons(s)
             assert np.array_equal(ge, e) and np.array_equal(go, o), s
             assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
+
+
+@pytest.mark.parametrize("L,nr,nc,ns,split,pipe", [(40, 64, 6, 2, 0, 0), (96, 64, 6, 2, 1, 0),
+                                                   (56, 32, 3, 1, 0, 1), (96, 128, 2, 2, 0, 1)])
+def test_whole_row_blocks_match_oracle(L, nr, nc, ns, split, pipe):
+    """Sweep blocks spanning whole rows along x (tile=row; L/4 threads per
+    row, the last y tile partly empty), direct and pipelined loads, against
+    the oracle over every walk shift."""
+    old = _pinned({"MICSA_SWEEP_ZC": "4", "MICSA_SWEEP_PD": "2", "MICSA_SWEEP_PIPE": str(pipe),
+                   "MICSA_SWEEP_TILE": "row", "MICSA_SWEEP_SPLIT": str(split),
+                   "MICSA_SWEEP_OCC": "3", "MICSA_RESIDENT": "0"})
+    try:
+        ctx = micsa.Context(L, nr, ns, nc)
+        assert "tile=row" in ctx.tuning(), ctx.tuning()
+    finally:
+        _restore(old)
+    rng = np.random.default_rng(13 * L + ns + pipe)
+    st = random_state(rng, L, nr, nc, ns)
+    iters = L // 2 + 3
+    with ctx:
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            ctx.upload_couplings(s, J)
+            ctx.upload_spins(s, e, o)
+            ctx.upload_demons(s, w0, w1)
+        ctx.iterate(iters)
+        ctx.synchronize()
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            for _ in range(iters):
+                oracle.micsa_iteration(L, nr, nc, J, e, o, w0, w1, 8)
+            ge, go = ctx.download_spins(s)
+            g0, g1 = ctx.download_demons(s)
+            assert np.array_equal(ge, e) and np.array_equal(go, o), s
+            assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
