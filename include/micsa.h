@@ -267,10 +267,48 @@ typedef struct {
  * time after the start; contexts are created before the start).  Outputs as
  * micsa_run_batch's (offsets over the requests in the given order); res[j]
  * receives the request's times; seconds (optional) the time of the last
- * finish. */
+ * finish.  A replay of the trace through a micsa_server (below). */
 int micsa_serve(const micsa_serve_config *cfg, const micsa_request *req, int n,
                 micsa_request_result *res, int32_t *e_spin, uint64_t *e_demon, double *seconds,
                 char *err, size_t errlen);
+
+/* A long-lived server for callers that produce requests as they go: the
+ * same pools, slots and rounds as micsa_serve, fed by micsa_submit from any
+ * thread.  The shapes it serves are fixed at creation (their contexts are
+ * created and tuned then, sized so that all fit hbm_budget). */
+typedef struct micsa_server micsa_server;
+typedef struct {
+  int L, nr, nc;
+  int slots; /* sample slots of this shape's context (0: as many as the budget allows,
+                at most slots_max) */
+} micsa_pool_shape;
+typedef struct {
+  int device;
+  int64_t hbm_budget;  /* bytes all contexts may hold together (0: 48 GiB) */
+  int slots_max;       /* slots per shape (0: 64) */
+  int64_t chunk;       /* most iterations per round (0: 1024) */
+  int prep_threads;    /* host threads initialising requests (0: cores - 1) */
+  const micsa_pool_shape *shapes;
+  int nshapes;
+} micsa_server_config;
+int micsa_server_create(const micsa_server_config *cfg, micsa_server **out, char *err,
+                        size_t errlen);
+/* Queue one job; *id identifies it in micsa_poll.  MICSA_ERR_UNSUPPORTED if
+ * the server has no pool of the job's shape; a pool that failed returns its
+ * error for its shape from then on. */
+int micsa_submit(micsa_server *sv, const micsa_job *job, int64_t *id);
+/* Wait up to timeout_s seconds (0: just look) for request id.  *done = 1 when
+ * it has finished: its measurements are copied out (e_spin
+ * [micsa_job_measurements(iterations) * nr] and e_demon likewise, either may
+ * be NULL), times (optional) receives the seconds from its submission to its
+ * initialisation, admission and finish, and the id is released.  A request
+ * whose pool failed returns that error (and is released).  Unknown or
+ * released ids: MICSA_ERR_ARG. */
+int micsa_poll(micsa_server *sv, int64_t id, double timeout_s, int *done, int32_t *e_spin,
+               uint64_t *e_demon, micsa_request_result *times);
+/* Let every submitted request finish, stop the threads and free the
+ * contexts; results not yet polled are dropped.  NULL is accepted. */
+int micsa_server_destroy(micsa_server *sv);
 
 /* Per-sample run flags, active[s] != 0 = sample s runs (all, after
  * micsa_create; NULL restores that).  A frozen sample is skipped by the

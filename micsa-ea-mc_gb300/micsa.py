@@ -26,6 +26,7 @@ ABI_SYMBOLS = [
     "micsa_download_demons", "micsa_profile", "micsa_tuning_report", "micsa_energy_noalloc",
     "micsa_synchronize", "micsa_kernel_launches", "micsa_stream", "micsa_job_measurements",
     "micsa_run_batch", "micsa_set_active", "micsa_serve", "micsa_job_beta",
+    "micsa_server_create", "micsa_submit", "micsa_poll", "micsa_server_destroy",
 ]
 NOALLOC_MAX_REPLICAS = 8192
 
@@ -71,6 +72,17 @@ class RequestResult(C.Structure):
 class ServeConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget", C.c_int64), ("slots_max", C.c_int),
                 ("chunk", C.c_int64), ("prep_threads", C.c_int)]
+
+
+class PoolShape(C.Structure):
+    """micsa_pool_shape: one shape a server serves (slots 0 = from the budget)."""
+    _fields_ = [("L", C.c_int), ("nr", C.c_int), ("nc", C.c_int), ("slots", C.c_int)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget", C.c_int64), ("slots_max", C.c_int),
+                ("chunk", C.c_int64), ("prep_threads", C.c_int),
+                ("shapes", C.POINTER(PoolShape)), ("nshapes", C.c_int)]
 
 
 class RefreshPlan(C.Structure):
@@ -142,6 +154,12 @@ def lib():
                                   C.c_char_p, C.c_size_t]),
         "micsa_run_batch": (C.c_int, [C.c_int, C.POINTER(Job), C.c_int, i32p, u64p,
                                       C.POINTER(C.c_double), C.c_char_p, C.c_size_t]),
+        "micsa_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p),
+                                          C.c_char_p, C.c_size_t]),
+        "micsa_submit": (C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(C.c_int64)]),
+        "micsa_poll": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(C.c_int), i32p,
+                                 u64p, C.POINTER(RequestResult)]),
+        "micsa_server_destroy": (C.c_int, [C.c_void_p]),
         # host side (micsa-ea-mc_gb300/host/micsa_host.h)
         "micsa_check_seed": (C.c_uint64, [C.c_uint64]),
         "micsa_init_cpu_generators": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), u32p, C.c_uint64]),
@@ -539,6 +557,69 @@ def serve(requests, device=0, hbm_budget=0, slots_max=0, chunk=0, prep_threads=0
     e_s = [es[a:b].reshape(nm, r["nr"]) for a, b, nm, r in zip(cut[:-1], cut[1:], nms, requests)]
     e_d = [ed[a:b].reshape(nm, r["nr"]) for a, b, nm, r in zip(cut[:-1], cut[1:], nms, requests)]
     return e_s, e_d, [(x.prepared, x.admitted, x.finished) for x in res], sec.value
+
+
+class Server:
+    """A micsa_server: pools for the given shapes [(L, nr, nc) or (L, nr, nc,
+    slots)], jobs submitted as dicts (the micsa_job fields), results polled."""
+
+    def __init__(self, shapes, device=0, hbm_budget=0, slots_max=0, chunk=0, prep_threads=0):
+        sh = [tuple(x) + (0,) * (4 - len(x)) for x in shapes]
+        self._shapes = (PoolShape * len(sh))(*[PoolShape(*x) for x in sh])
+        cfg = ServerConfig(device, hbm_budget, slots_max, chunk, prep_threads, self._shapes, len(sh))
+        self.h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        rc = lib().micsa_server_create(C.byref(cfg), C.byref(self.h), err, 512)
+        if rc != MICSA_OK:
+            raise MicsaError("micsa_server_create: %s %s" % (STATUS.get(rc, rc), err.value.decode()))
+        self._jobs = {}
+
+    def submit(self, j):
+        job = Job(j["L"], j["nr"], j["nc"], j["iterations"], j["seed_J"], j["seed_u"], j["beta"],
+                  j.get("beta_end", 0.0))
+        i = C.c_int64()
+        rc = lib().micsa_submit(self.h, C.byref(job), C.byref(i))
+        if rc != MICSA_OK:
+            raise MicsaError("micsa_submit: %s" % STATUS.get(rc, rc))
+        self._jobs[i.value] = j
+        return i.value
+
+    def poll(self, i, timeout=0.0):
+        """None while request i runs; then (e_spin [m, nr], e_demon [m, nr],
+        (prepared, admitted, finished) seconds after its submission)."""
+        j = self._jobs.get(i)
+        nm = lib().micsa_job_measurements(j["iterations"]) if j else 0
+        nr = j["nr"] if j else 0
+        es = np.zeros(max(1, nm * nr), np.int32)
+        ed = np.zeros(max(1, nm * nr), np.uint64)
+        done, t = C.c_int(), RequestResult()
+        rc = lib().micsa_poll(self.h, i, timeout, C.byref(done), _ptr(es, C.c_int32),
+                              _ptr(ed, C.c_uint64), C.byref(t))
+        if rc != MICSA_OK:
+            self._jobs.pop(i, None)
+            raise MicsaError("micsa_poll: %s" % STATUS.get(rc, rc))
+        if not done.value:
+            return None
+        del self._jobs[i]
+        return (es[:nm * nr].reshape(nm, nr), ed[:nm * nr].reshape(nm, nr),
+                (t.prepared, t.admitted, t.finished))
+
+    def close(self):
+        if self.h:
+            lib().micsa_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def correlation_lengths(L, c4):
