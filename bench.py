@@ -253,7 +253,10 @@ def run_micsa(a, dist):
     achieved = per_launch / (sweep_ms * 1e-3) / 1e9
     peak, kind = peaks()
     traffic, tnote = traffic_per_launch(L, nr, ns)
-    roof = {"bound": "hbm", "kernel": "k_sweep<2,true> (micSA half-sweep)",
+    kernel = ("k_sweep_dep (dataflow sweep: the %d half-sweeps of an iteration in one launch; "
+              "time per half-sweep)" % (2 * nc) if "load=flow" in ctx.tuning()
+              else "k_sweep (micSA half-sweep)")
+    roof = {"bound": "hbm", "kernel": kernel,
             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": kind,
             "algorithmic_bytes_per_launch": int(per_launch),

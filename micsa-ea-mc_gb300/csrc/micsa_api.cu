@@ -23,7 +23,7 @@
 #include "micsa_jump.h"
 #include "micsa_kernels.cuh"
 
-#define MICSA_TUNE_MAX 320
+#define MICSA_TUNE_MAX 400
 
 struct micsa_ctx {
   micsa_config cfg;
@@ -34,6 +34,7 @@ struct micsa_ctx {
   uint32_t *te = nullptr, *keys = nullptr;
   int *walk = nullptr;
   uint8_t *active = nullptr; /* per-sample flags, 1 = runs */
+  unsigned *flow_ctl = nullptr; /* counters of the dataflow sweep: 4 + ns*L words */
   uint64_t *stage = nullptr;
   unsigned long long *acc = nullptr;
   size_t stage_words = 0, acc_words = 0;
@@ -203,10 +204,16 @@ cudaError_t launch_half(micsa_ctx *ctx, const micsa_geo &g, int s, int p, int ic
 /* The half-sweeps of one iteration (ic = ic0 .. ic1-1).  split = 0: plane by
  * plane, all samples per launch.  split = 1: sample-major, all of sample 0's
  * half-sweeps, then sample 1's, ...: the spins that stay hot in L2 across
- * consecutive launches are one sample's. */
+ * consecutive launches are one sample's.  g.flow (whole iterations): one
+ * dataflow launch, its tiles in the same two orders. */
 cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0, int ic1,
                           int64_t *launches) {
   cudaError_t e = cudaSuccess;
+  if (g.flow && ic0 == 0 && ic1 == g.nc) { /* the whole iteration in one dataflow launch */
+    if (launches) ++*launches;
+    return micsa_launch_sweep_flow(g, split, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb, ctx->walk,
+                                   ctx->flow_ctl, ctx->stream);
+  }
   if (!split) {
     for (int ic = ic0; ic < ic1; ic++)
       for (int p = 0; p < 2; p++)
@@ -225,7 +232,7 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
  * choice and table instead of timing again, so batches and servers that open
  * many contexts of a few shapes pay for each shape once. */
 struct tune_entry {
-  int zc, pd, split, occ, tma, async, pipe, tw, n;
+  int zc, pd, split, occ, tma, async, pipe, tw, flow, n;
   std::vector<int> zcs, pds, splits, occs, tmas, tws;
   std::vector<double> ms;
 };
@@ -266,12 +273,14 @@ int autotune(micsa_ctx *ctx) {
     g.pd = pd;
     const char *es = getenv("MICSA_SWEEP_SPLIT"), *eo = getenv("MICSA_SWEEP_OCC"),
                *et = getenv("MICSA_SWEEP_TMA"), *ea = getenv("MICSA_SWEEP_ASYNC"),
-               *ep2 = getenv("MICSA_SWEEP_PIPE"), *ew = getenv("MICSA_SWEEP_TILE");
+               *ep2 = getenv("MICSA_SWEEP_PIPE"), *ew = getenv("MICSA_SWEEP_TILE"),
+               *ef = getenv("MICSA_SWEEP_FLOW");
     ctx->split = es && atoi(es) && g.ns > 1;
     g.tma = et && atoi(et) && ctx->tma.ok;
     g.async = ea && atoi(ea) && g.W == 2 && !g.tma;
     g.pipe = ep2 && atoi(ep2) && !g.tma && !g.async;
     g.tw = ew && !strcmp(ew, "row") && !g.tma && micsa_sweep_wide_differs(g.L);
+    g.flow = ef && atoi(ef) && !g.tma && !g.async && !g.pipe;
     const int oc = eo ? atoi(eo) : 3;
     g.occ = g.pipe ? (oc == 2 ? 2 : 3) : (oc == 4 ? 4 : 3);
     ctx->ntune = 0;
@@ -292,6 +301,7 @@ int autotune(micsa_ctx *ctx) {
       g.async = t.async;
       g.pipe = t.pipe;
       g.tw = t.tw;
+      g.flow = t.flow;
       ctx->ntune = t.n;
       for (int c = 0; c < t.n; c++) {
         ctx->tune_zc[c] = t.zcs[c];
@@ -311,14 +321,15 @@ int autotune(micsa_ctx *ctx) {
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
   int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, best_tma = 0;
-  int best_async = 0, best_pipe = 0, best_tw = 0, n = 0;
+  int best_async = 0, best_pipe = 0, best_tw = 0, best_flow = 0, n = 0;
   const int ntw = micsa_sweep_wide_differs(g.L) ? 2 : 1;
   const int reps = 3;
   const int nocc = g.W % 4 ? 2 : 1; /* the 4-blocks variant exists for VW <= 2 */
   /* tm: 0 direct loads, 1 TMA-staged demon tiles, 2 cp.async double buffer (W = 2),
    * 3 loads pipelined one step ahead in registers (register budget for 3 or 2
-   * blocks per SM instead of 3 or 4) */
-  for (int tm = 0; tm < 4; tm++)
+   * blocks per SM instead of 3 or 4), 4 direct loads in one dataflow launch
+   * per iteration (split: its tiles sample-major or half-sweep-major) */
+  for (int tm = 0; tm < 5; tm++)
   for (int tw = 0; tw < ntw; tw++)
   for (int oc = 0; oc < nocc; oc++)
   for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
@@ -335,6 +346,7 @@ int autotune(micsa_ctx *ctx) {
       g.async = tm == 2;
       g.pipe = tm == 3;
       g.tw = tw;
+      g.flow = tm == 4;
       /* one iteration's half-sweeps in their launch order, captured and
        * replayed as a graph the way micsa_iterate runs them: timed launch by
        * launch, small lattices would measure the host's launch rate */
@@ -381,6 +393,7 @@ int autotune(micsa_ctx *ctx) {
         best_async = g.async;
         best_pipe = g.pipe;
         best_tw = g.tw;
+        best_flow = g.flow;
       }
     }
   ctx->ntune = n;
@@ -392,6 +405,7 @@ int autotune(micsa_ctx *ctx) {
   g.async = best_async;
   g.pipe = best_pipe;
   g.tw = best_tw;
+  g.flow = best_flow;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (use_cache) {
@@ -404,6 +418,7 @@ int autotune(micsa_ctx *ctx) {
     t.async = g.async;
     t.pipe = g.pipe;
     t.tw = g.tw;
+    t.flow = g.flow;
     t.n = n;
     t.zcs.assign(ctx->tune_zc, ctx->tune_zc + n);
     t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
@@ -467,6 +482,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.async = 0;
   g.pipe = 0;
   g.tw = 0;
+  g.flow = 0;
   {
     /* MICSA_PDL=0: plain launches of the sweeps */
     const char *e = getenv("MICSA_PDL");
@@ -511,6 +527,9 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   MICSA_CK_CREATE(cudaMalloc(&ctx->acc, 8 * ctx->acc_words));
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->walk, 0, sizeof(int) * MICSA_MAX_SAMPLES, ctx->stream));
   MICSA_CK_CREATE(cudaMalloc(&ctx->active, (size_t)cfg->nsamples));
+  MICSA_CK_CREATE(cudaMalloc(&ctx->flow_ctl, sizeof(unsigned) * (4 + (size_t)cfg->nsamples * cfg->L)));
+  MICSA_CK_CREATE(cudaMemsetAsync(ctx->flow_ctl, 0,
+                                  sizeof(unsigned) * (4 + (size_t)cfg->nsamples * cfg->L), ctx->stream));
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->active, 1, (size_t)cfg->nsamples, ctx->stream));
   g.active = ctx->active;
   MICSA_CK_CREATE(cudaMemsetAsync(ctx->spin, 0, 4 * s.spin_w, ctx->stream));
@@ -546,7 +565,7 @@ int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
   int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s%s |", ctx->g.zc,
                    ctx->g.pd, ctx->split, ctx->g.occ,
-                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : "direct")),
+                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : (ctx->g.flow ? "flow" : "direct"))),
                    ctx->g.tw ? "row" : "default", ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
     k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],
@@ -574,7 +593,7 @@ int micsa_destroy(micsa_ctx *ctx) {
   void *bufs[] = {ctx->spin, ctx->dem0,     ctx->dem1,    ctx->rnd,      ctx->jb,
                   ctx->lut,  ctx->te,       ctx->keys,    ctx->walk,     ctx->stage,
                   ctx->acc,  ctx->plan_lcg, ctx->plan_xo, ctx->plan_fib, ctx->rec,
-                  ctx->active};
+                  ctx->active, ctx->flow_ctl};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1089,6 +1108,8 @@ int micsa_synchronize(micsa_ctx *ctx) {
   unsigned to = 0;
   MICSA_CK(micsa_tma_timeout_count(&to));
   if (to) return fail(ctx, MICSA_ERR_CUDA, "%u staged demon loads timed out (read directly)", to);
+  MICSA_CK(micsa_flow_timeout_count(&to));
+  if (to) return fail(ctx, MICSA_ERR_CUDA, "%u waits of the dataflow sweep timed out", to);
   return MICSA_OK;
 }
 

@@ -35,11 +35,16 @@ __device__ __forceinline__ uint64_t l2_stream() {
 }
 
 /* loads/stores with an L2 cache policy: nc = read-only (non-coherent) path,
- * na = no L1 allocation (data used once) */
+ * na = no L1 allocation (data used once), co = coherent load the compiler
+ * may schedule freely (for words other blocks of the same launch write,
+ * ordered by an acquire before the address is known) */
 template <int VW> struct hint;
 template <> struct hint<1> {
   static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[1], uint64_t pol) {
     asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(o[0]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void ld_co(const uint32_t *a, uint32_t (&o)[1], uint64_t pol) {
+    asm("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(o[0]) : "l"(a), "l"(pol));
   }
   static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[1], uint64_t pol) {
     asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(o[0]) : "l"(a), "l"(pol));
@@ -55,6 +60,10 @@ template <> struct hint<1> {
 template <> struct hint<2> {
   static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[2], uint64_t pol) {
     asm("ld.global.nc.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
+        : "=r"(o[0]), "=r"(o[1]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void ld_co(const uint32_t *a, uint32_t (&o)[2], uint64_t pol) {
+    asm("ld.global.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
         : "=r"(o[0]), "=r"(o[1]) : "l"(a), "l"(pol));
   }
   static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[2], uint64_t pol) {
@@ -73,6 +82,10 @@ template <> struct hint<2> {
 template <> struct hint<4> {
   static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[4], uint64_t pol) {
     asm("ld.global.nc.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+        : "=r"(o[0]), "=r"(o[1]), "=r"(o[2]), "=r"(o[3]) : "l"(a), "l"(pol));
+  }
+  static __device__ __forceinline__ void ld_co(const uint32_t *a, uint32_t (&o)[4], uint64_t pol) {
+    asm("ld.global.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
         : "=r"(o[0]), "=r"(o[1]), "=r"(o[2]), "=r"(o[3]) : "l"(a), "l"(pol));
   }
   static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[4], uint64_t pol) {
@@ -236,12 +249,14 @@ __device__ unsigned int micsa_tma_timeouts;
 template <int VW> struct pair_io;
 template <> struct pair_io<1> {
   static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[2], uint64_t p) { hint<2>::ld_nc(a, o, p); }
+  static __device__ __forceinline__ void ld_co(const uint32_t *a, uint32_t (&o)[2], uint64_t p) { hint<2>::ld_co(a, o, p); }
   static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[2], uint64_t p) { hint<2>::ld(a, o, p); }
   static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t (&o)[2], uint64_t p) { hint<2>::ld_na(a, o, p); }
   static __device__ __forceinline__ void st(uint32_t *a, const uint32_t (&o)[2], uint64_t p) { hint<2>::st(a, o, p); }
 };
 template <> struct pair_io<2> {
   static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[4], uint64_t p) { hint<4>::ld_nc(a, o, p); }
+  static __device__ __forceinline__ void ld_co(const uint32_t *a, uint32_t (&o)[4], uint64_t p) { hint<4>::ld_co(a, o, p); }
   static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[4], uint64_t p) { hint<4>::ld(a, o, p); }
   static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t (&o)[4], uint64_t p) { hint<4>::ld_na(a, o, p); }
   static __device__ __forceinline__ void st(uint32_t *a, const uint32_t (&o)[4], uint64_t p) { hint<4>::st(a, o, p); }
@@ -257,6 +272,9 @@ template <> struct pair_io<4> {
   }
   static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t (&o)[8], uint64_t p) {
     uint32_t x[4], y[4]; hint<4>::ld_nc(a, x, p); hint<4>::ld_nc(a + 4, y, p); join(o, x, y);
+  }
+  static __device__ __forceinline__ void ld_co(const uint32_t *a, uint32_t (&o)[8], uint64_t p) {
+    uint32_t x[4], y[4]; hint<4>::ld_co(a, x, p); hint<4>::ld_co(a + 4, y, p); join(o, x, y);
   }
   static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t (&o)[8], uint64_t p) {
     uint32_t x[4], y[4]; hint<4>::ld(a, x, p); hint<4>::ld(a + 4, y, p); join(o, x, y);
@@ -294,6 +312,17 @@ template <int VW, bool WIDE> struct pairs {
     uint32_t x[VW], y[VW];
     hint<VW>::ld_nc(a, x, p); hint<VW>::ld_nc(a + W, y, p); cat(o, x, y);
   }
+  static __device__ __forceinline__ void ld_co(const uint32_t *a, uint32_t W, uint32_t (&o)[N], uint64_t p) {
+    if (WIDE) { pair_io<VW>::ld_co(a, o, p); return; }
+    uint32_t x[VW], y[VW];
+    hint<VW>::ld_co(a, x, p); hint<VW>::ld_co(a + W, y, p); cat(o, x, y);
+  }
+  /* the other colour's words: read-only in a plain half-sweep launch, written
+   * by other tiles of the same launch in the dataflow sweep */
+  template <bool FLOW>
+  static __device__ __forceinline__ void ld_oth(const uint32_t *a, uint32_t W, uint32_t (&o)[N], uint64_t p) {
+    if (FLOW) ld_co(a, W, o, p); else ld_nc(a, W, o, p);
+  }
   static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t W, uint32_t (&o)[N], uint64_t p) {
     if (WIDE) { pair_io<VW>::ld(a, o, p); return; }
     uint32_t x[VW], y[VW];
@@ -321,28 +350,24 @@ template <int VW, bool WIDE> struct pairs {
  * bytes and the two demon words per plane.  Block = (TX pairs along x/2) x
  * (TY rows); TX divides L/4; grid = (L/4/TX, ytiles*ns*G, L/zc).
  * In-plane offsets are 32-bit (P*W < 2^32 is checked at creation). */
-template <int VW, bool MICSA, bool WIDE, int MINB, bool TMA>
-__global__ void __launch_bounds__(TPB, MINB)
-k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
-        const int zc, const int pd, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
-        uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
-        const int *__restrict__ walk, const uint32_t *__restrict__ rnd,
-        const __grid_constant__ micsa_tma tm) {
+/* One block's tile of a half-sweep: sample s, word group grp, row tile
+ * `tile`, x block bx, z planes [z0, z0 + zc), demon walk kwalk.  FLOW: the
+ * other colour is read through the coherent path (other tiles of the same
+ * dataflow launch write it). */
+template <int VW, bool MICSA, bool WIDE, bool TMA, bool FLOW>
+__device__ __forceinline__ void sweep_block(
+    const micsa_geo &g, const int p, const int ic, const uint32_t s, const uint32_t grp,
+    const uint32_t tile, const uint32_t bx, const uint32_t z0, const int zc, const int pd,
+    const int kwalk, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
+    uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb, const uint32_t *__restrict__ rnd,
+    const micsa_tma &tm) {
   constexpr int N = 2 * VW; /* words per pair */
-  grid_dependency_sync();
   using PR = pairs<VW, WIDE>;
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
-  const uint32_t by = blockIdx.y;
-  const uint32_t tile = by % ytiles, sg = by / ytiles; /* block-uniform */
-  const uint32_t s = sg / G, grp = sg % G;
-  /* the walk and the run flag are loaded together: one round trip */
-  const int kwalk = MICSA ? __ldg(walk + s) : 0;
-  if (micsa_frozen(g, (int)s)) return;
   const uint32_t y = tile * blockDim.y + threadIdx.y;
   if (y >= L) return;
-  const uint32_t xa = 2 * (blockIdx.x * blockDim.x + threadIdx.x); /* x/2 of site A */
+  const uint32_t xa = 2 * (bx * blockDim.x + threadIdx.x); /* x/2 of site A */
   const uint32_t plane = L * Lh;
-  const uint32_t z0 = blockIdx.z * zc;
   const uint32_t row = y * Lh + xa;
   const uint32_t rowN = (y + 1 == L) ? xa : row + Lh;
   const uint32_t rowS = (y == 0) ? row + (L - 1) * Lh : row - Lh;
@@ -400,7 +425,7 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
     const int k = kwalk;
     const int sh = ((p == 0) == (ic < 3)) ? k : -k;
     const int axis = ic < 3 ? ic : ic - 3;
-    const int xb = 2 * blockIdx.x * blockDim.x, yb = tile * blockDim.y;
+    const int xb = 2 * bx * blockDim.x, yb = tile * blockDim.y;
     int cx = xb, ry = yb;
     if (axis == 0) { cx = xb - sh; cx += cx < 0 ? (int)Lh : (cx >= (int)Lh ? -(int)Lh : 0); }
     if (axis == 1) { ry = yb - 2 * sh; ry += ry < 0 ? (int)L : (ry >= (int)L ? -(int)L : 0); }
@@ -433,8 +458,8 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
 
   /* other colour at (2j, 2j+1; y) for planes z0-1 and z0 */
   uint32_t vm[N], v0[N];
-  PR::ld_nc(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, W, vm, keep);
-  PR::ld_nc(oth + (z0 * plane + row) * W, W, v0, keep);
+  PR::template ld_oth<FLOW>(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, W, vm, keep);
+  PR::template ld_oth<FLOW>(oth + (z0 * plane + row) * W, W, v0, keep);
 
   uint32_t zdd = zd;
 #pragma unroll 2
@@ -444,10 +469,13 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
     const uint32_t rowoff = (y + z + p) & 1; /* x = 2*(x/2) + rowoff for both */
     uint32_t own[N], up[N], vn[N], vs[N], ext[VW], a0[N], a1[N], a2[N];
     PR::ld(mine + (zo + row) * W, W, own, keep);
-    PR::ld_nc(oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, W, up, keep);
-    PR::ld_nc(oth + (zo + rowN) * W, W, vn, keep);
-    PR::ld_nc(oth + (zo + rowS) * W, W, vs, keep);
-    hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
+    PR::template ld_oth<FLOW>(oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, W, up, keep);
+    PR::template ld_oth<FLOW>(oth + (zo + rowN) * W, W, vn, keep);
+    PR::template ld_oth<FLOW>(oth + (zo + rowS) * W, W, vs, keep);
+    if (FLOW)
+      hint<VW>::ld_co(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
+    else
+      hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
     const uint32_t jb2 = ld_u16_keep(jbp + zo + row, keep);
     bool from_smem = false;
     if (TMA && staged) {
@@ -552,6 +580,182 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
       v0[w] = up[w];
     }
     zdd = (zdd + 1 == L) ? 0 : zdd + 1;
+  }
+}
+
+template <int VW, bool MICSA, bool WIDE, int MINB, bool TMA>
+__global__ void __launch_bounds__(TPB, MINB)
+k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
+        const int zc, const int pd, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
+        uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
+        const int *__restrict__ walk, const uint32_t *__restrict__ rnd,
+        const __grid_constant__ micsa_tma tm) {
+  grid_dependency_sync();
+  const uint32_t by = blockIdx.y;
+  const uint32_t tile = by % ytiles, sg = by / ytiles; /* block-uniform */
+  const uint32_t s = sg / G, grp = sg % G;
+  /* the walk and the run flag are loaded together: one round trip */
+  const int kwalk = MICSA ? __ldg(walk + s) : 0;
+  if (micsa_frozen(g, (int)s)) return;
+  sweep_block<VW, MICSA, WIDE, TMA, false>(g, p, ic, s, grp, tile, blockIdx.x, blockIdx.z * zc, zc,
+                                           pd, kwalk, spin, d0, d1, jb, rnd, tm);
+}
+
+/* ---------------------------------------------------- dataflow sweep */
+/* All 2*nc half-sweeps of one iteration, of every sample, in one launch:
+ * the launch boundaries between half-sweeps (each a drain of the whole GPU)
+ * become per-slab dependencies.  The grid has one block per tile -- one
+ * k_sweep block over one slab of zc z planes -- and a block takes its tile
+ * from a ticket counter when it starts (not from blockIdx, whose dispatch
+ * order is not guaranteed), in this order: sample then half-sweep j
+ * (sample-major, the L2 then holds one sample's spins) or half-sweep then
+ * sample (many small samples side by side), then slab (the half-sweep's
+ * slabs start at slab j mod L/zc), then tile.  Half-sweep j has ic = j/2
+ * and colour p = j%2, the order of the reference's Monte_Carlo loop
+ * (main.cu:254-284).
+ *
+ * A tile of half-sweep j on slab b reads the other colour on planes
+ * z0-1 .. z0+zc and its demon slots, and writes its own colour on slab b.
+ * It starts once half-sweep j-1 has finished slabs b-1, b and b+1, so it
+ * reads exactly what the j-th half-sweep of the reference reads; and no tile
+ * still running reads what it writes (a tile of j+k runs beside one of j
+ * only more than k slabs away, and reads one plane beyond its slab).  The
+ * demon walk moves by whole iterations, between launches.
+ *
+ * Counters: ctl[0] tickets, ctl[1] blocks done, ctl[4 + s*nslab + b] tiles
+ * of slab b of sample s finished in this launch.  No tile of j starts on
+ * slab b before all of slab b's tiles of j-1 are done, so slab b has
+ * finished half-sweeps 0 .. j-1 exactly when its counter reaches (tiles per
+ * slab) * j.  Tiles wait only on earlier tickets, and a ticket is only held
+ * by a running block, so the earliest unfinished tile can always run: the
+ * launch needs no co-residency.  The lead thread polls the three counters
+ * with relaxed loads issued together, then an acquire fence and a block
+ * barrier order the tile's loads after the producers' stores; a producer
+ * releases with a block barrier, a fence and an atomic add.  Waits are
+ * bounded (2 s by the global timer; after one runs out every later wait
+ * gives up at once, and micsa_flow_timeouts counts them); the last block to
+ * finish resets the counters for the next launch. */
+__device__ unsigned int micsa_flow_timeouts;
+
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *a) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+/* wait until *a, *b and *c are all >= need, then acquire; false when the
+ * limit ran out (or an earlier wait's did) */
+__device__ __forceinline__ bool flow_wait3(const unsigned *a, const unsigned *b,
+                                           const unsigned *c, unsigned need) {
+  uint64_t t0 = 0;
+  bool ok = true;
+  for (;;) {
+    const unsigned x = ld_relaxed_u32(a), y = ld_relaxed_u32(b), z = ld_relaxed_u32(c);
+    if (min(x, min(y, z)) >= need) break;
+    if (!t0) t0 = global_ns();
+    if (*(volatile unsigned *)&micsa_flow_timeouts || global_ns() - t0 > 2000000000ull) {
+      ok = false;
+      break;
+    }
+    __nanosleep(64);
+  }
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+  return ok;
+}
+
+/* The lead thread's part: take a ticket, decode it into job[] (s, j, slab,
+ * bx, row tile, group, walk) from the launch's constants in cst[] and wait
+ * for the tile's dependencies. */
+enum { C_GX, C_NSLAB, C_T, C_PER_HALF, C_PER_SAMPLE, C_YT, C_SMAJ, C_N };
+__device__ __forceinline__ void dep_take(const micsa_geo &g, const int *__restrict__ walk,
+                                         unsigned *__restrict__ ctl, const unsigned *cst,
+                                         unsigned *job) {
+  const unsigned u = atomicAdd(ctl, 1u);
+  const unsigned nslab = cst[C_NSLAB], T = cst[C_T], gx = cst[C_GX], ytiles = cst[C_YT];
+  unsigned s, j, r2;
+  if (cst[C_SMAJ]) {
+    s = u / cst[C_PER_SAMPLE];
+    const unsigned r = u % cst[C_PER_SAMPLE];
+    j = r / cst[C_PER_HALF];
+    r2 = r % cst[C_PER_HALF];
+  } else {
+    const unsigned per_j = (unsigned)g.ns * cst[C_PER_HALF], r = u % per_j;
+    j = u / per_j;
+    s = r / cst[C_PER_HALF];
+    r2 = r % cst[C_PER_HALF];
+  }
+  const unsigned b = (r2 / T + j) % nslab, t = r2 % T;
+  job[0] = s;
+  job[1] = j;
+  job[2] = b;
+  job[3] = t % gx;
+  job[4] = (t / gx) % ytiles;
+  job[5] = t / (gx * ytiles);
+  job[6] = (unsigned)__ldg(walk + s);
+  if (j > 0 && !micsa_frozen(g, (int)s)) {
+    const unsigned *c = ctl + 4 + s * nslab;
+    if (!flow_wait3(c + (b == 0 ? nslab - 1 : b - 1), c + b, c + (b + 1 == nslab ? 0 : b + 1),
+                    T * j))
+      atomicAdd(&micsa_flow_timeouts, 1u);
+  }
+}
+
+/* The tile's values go through shared memory and are read where they are
+ * used, so that none of them stays in a register across the sweep body
+ * (which needs about all of the 64 registers of the 4-blocks budget). */
+template <int VW, bool WIDE, int MINB>
+__global__ void __launch_bounds__(TPB, MINB)
+k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, const int zc,
+            const int pd, const int smaj, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
+            uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
+            const int *__restrict__ walk, unsigned *__restrict__ ctl) {
+  grid_dependency_sync();
+  __shared__ unsigned cst[C_N];
+  __shared__ unsigned job[8]; /* s, j, slab, bx, row tile, group, walk, last */
+  const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+  if (lead) {
+    const unsigned gx = (unsigned)g.Lh / 2u / blockDim.x; /* blocks along x */
+    const unsigned nslab = (unsigned)(g.L / zc);
+    const unsigned T = gx * (unsigned)ytiles * (unsigned)G; /* tiles per slab */
+    cst[C_GX] = gx;
+    cst[C_NSLAB] = nslab;
+    cst[C_T] = T;
+    cst[C_YT] = (unsigned)ytiles;
+    cst[C_PER_HALF] = nslab * T;
+    cst[C_PER_SAMPLE] = 2u * (unsigned)g.nc * nslab * T;
+    cst[C_SMAJ] = (unsigned)smaj;
+    dep_take(g, walk, ctl, cst, job);
+  }
+  __syncthreads();
+  {
+    const unsigned s = job[0], j = job[1];
+    if (!micsa_frozen(g, (int)s)) {
+      micsa_tma none;
+      sweep_block<VW, true, WIDE, false, true>(g, (int)(j & 1u), (int)(j >> 1), s, job[5], job[4],
+                                               job[3], job[2] * (unsigned)zc, zc, pd, (int)job[6],
+                                               spin, d0, d1, jb, nullptr, none);
+    }
+  }
+  __syncthreads();
+  if (lead) {
+    __threadfence();
+    atomicAdd(ctl + 4 + job[0] * cst[C_NSLAB] + job[2], 1u);
+    __threadfence();
+    job[7] = atomicAdd(ctl + 1, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (job[7]) { /* every other block has finished: reset for the next launch */
+    const unsigned tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+    const unsigned n = (unsigned)g.ns * cst[C_NSLAB];
+    for (unsigned k = tid; k < n; k += nt) ctl[4 + k] = 0;
+    if (lead) {
+      ctl[0] = 0;
+      ctl[1] = 0;
+    }
   }
 }
 
@@ -1348,6 +1552,55 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
   }
 #undef MICSA_SWEEP
   return cudaGetLastError();
+}
+
+/* the dataflow sweep: one block per tile */
+template <int VW, bool WIDE, int MINB>
+static cudaError_t sweep_flow_k(const micsa_geo &g, int smaj, int ytiles, int G, int zc,
+                                dim3 block, int64_t tiles, uint32_t *spin, uint32_t *d0,
+                                uint32_t *d1, const uint8_t *jb, const int *walk, unsigned *ctl,
+                                cudaStream_t st) {
+  return launch_sweep(g, k_sweep_dep<VW, WIDE, MINB>, dim3((unsigned)tiles), block, 0, st, g,
+                      ytiles, G, zc, g.pd, smaj, spin, d0, d1, jb, walk, ctl);
+}
+
+template <int VW>
+static cudaError_t sweep_flow_vw(const micsa_geo &g, int smaj, uint32_t *spin, uint32_t *d0,
+                                 uint32_t *d1, const uint8_t *jb, const int *walk, unsigned *ctl,
+                                 cudaStream_t st) {
+  const int G = g.W / VW;
+  int tx, ty;
+  sweep_tile(g.L, g.tw, &tx, &ty);
+  const int ytiles = (g.L + ty - 1) / ty;
+  const int zc = g.zc > 0 ? g.zc : 4;
+  if (g.L % zc) return cudaErrorInvalidValue;
+  const int64_t tiles = (int64_t)g.ns * 2 * g.nc * (g.L / zc) * (g.Lh / 2 / tx) * ytiles * G;
+  if (tiles >= (1LL << 31)) return cudaErrorInvalidValue; /* 32-bit tickets */
+  const dim3 block(tx, ty);
+  constexpr int B0 = VW == 4 ? 2 : 3, B1 = VW == 4 ? 2 : 4;
+  if (G == 1)
+    return g.occ == 4 ? sweep_flow_k<VW, true, B1>(g, smaj, ytiles, G, zc, block, tiles, spin, d0,
+                                                   d1, jb, walk, ctl, st)
+                      : sweep_flow_k<VW, true, B0>(g, smaj, ytiles, G, zc, block, tiles, spin, d0,
+                                                   d1, jb, walk, ctl, st);
+  return g.occ == 4 ? sweep_flow_k<VW, false, B1>(g, smaj, ytiles, G, zc, block, tiles, spin, d0,
+                                                  d1, jb, walk, ctl, st)
+                    : sweep_flow_k<VW, false, B0>(g, smaj, ytiles, G, zc, block, tiles, spin, d0,
+                                                  d1, jb, walk, ctl, st);
+}
+
+cudaError_t micsa_launch_sweep_flow(const micsa_geo &g, int sample_major, uint32_t *spin,
+                                    uint32_t *d0, uint32_t *d1, const uint8_t *jb,
+                                    const int *walk, unsigned *ctl, cudaStream_t st) {
+  cudaError_t e;
+  if (g.W % 4 == 0) e = sweep_flow_vw<4>(g, sample_major, spin, d0, d1, jb, walk, ctl, st);
+  else if (g.W % 2 == 0) e = sweep_flow_vw<2>(g, sample_major, spin, d0, d1, jb, walk, ctl, st);
+  else e = sweep_flow_vw<1>(g, sample_major, spin, d0, d1, jb, walk, ctl, st);
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t micsa_flow_timeout_count(unsigned *n) {
+  return cudaMemcpyFromSymbol(n, micsa_flow_timeouts, sizeof(unsigned));
 }
 
 cudaError_t micsa_make_tma(const micsa_geo &g, const uint32_t *d0, const uint32_t *d1,

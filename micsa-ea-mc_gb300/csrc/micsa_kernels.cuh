@@ -35,6 +35,7 @@ struct micsa_geo {
   int pipe;   /* 1: the sweep loads each z step's operands into registers one step ahead */
   int pdl;    /* 1: sweeps launched with programmatic dependent launch */
   int tw;     /* 1: sweep blocks span whole rows along x (when that differs) */
+  int flow;   /* 1: an iteration's half-sweeps run as one dataflow launch */
   int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */
@@ -74,6 +75,15 @@ cudaError_t micsa_launch_sweep_micsa(const micsa_geo &g, int p, int ic,
                                      uint32_t *spin, uint32_t *d0, uint32_t *d1,
                                      const uint8_t *jb, const int *walk,
                                      const micsa_tma *tm, cudaStream_t st);
+/* flag = 1: all 2*nc half-sweeps of one iteration of every sample in one
+ * launch (dataflow sweep, one block per tile), tiles taken sample-major or
+ * half-sweep-major; ctl = 4 + ns*L zeroed words of the context, left zeroed
+ * by the launch */
+cudaError_t micsa_launch_sweep_flow(const micsa_geo &g, int sample_major, uint32_t *spin,
+                                    uint32_t *d0, uint32_t *d1, const uint8_t *jb,
+                                    const int *walk, unsigned *ctl, cudaStream_t st);
+/* waits of the dataflow sweep that ran out since the process started */
+cudaError_t micsa_flow_timeout_count(unsigned *n);
 /* flag = 0 half-sweep of colour p with random words rnd[(k*P + i)*W + w] */
 cudaError_t micsa_launch_sweep_metropolis(const micsa_geo &g, int p,
                                           uint32_t *spin, const uint8_t *jb,

@@ -1,0 +1,115 @@
+"""The dataflow sweep -- all 2*nc half-sweeps of an iteration in one launch,
+one block per tile, tiles ordered by per-slab completion counters instead of
+launch boundaries -- pinned on, against the oracle: over more iterations
+than half the lattice side (every walk shift, and the counters reset by
+every launch), with 32, 64, 96 and 128 replicas, one, two, three slabs and
+many, default and whole-row blocks, both register budgets, tiles taken
+sample-major and half-sweep-major, frozen samples, and the headline shape."""
+import os
+
+import numpy as np
+import pytest
+
+import micsa
+import oracle
+from test_gpu_parity import random_state
+
+pytestmark = pytest.mark.gpu
+
+
+def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1):
+    env = {"MICSA_SWEEP_ZC": str(zc), "MICSA_SWEEP_PD": str(pd), "MICSA_SWEEP_FLOW": "1",
+           "MICSA_SWEEP_OCC": str(occ), "MICSA_SWEEP_SPLIT": str(split), "MICSA_RESIDENT": "0"}
+    if tile:
+        env["MICSA_SWEEP_TILE"] = tile
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        ctx = micsa.Context(L, nr, ns, nc)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    assert "load=flow" in ctx.tuning(), ctx.tuning()
+    return ctx
+
+
+def _upload(ctx, st):
+    for s, (J, e, o, w0, w1, _) in enumerate(st):
+        ctx.upload_couplings(s, J)
+        ctx.upload_spins(s, e, o)
+        ctx.upload_demons(s, w0, w1)
+
+
+def _check(ctx, st, L, nr, nc, iters, samples=None):
+    for s, (J, e, o, w0, w1, _) in enumerate(st):
+        if samples is not None and s not in samples:
+            continue
+        for _ in range(iters):
+            oracle.micsa_iteration(L, nr, nc, J, e, o, w0, w1, 8)
+        ge, go = ctx.download_spins(s)
+        g0, g1 = ctx.download_demons(s)
+        assert np.array_equal(ge, e) and np.array_equal(go, o), s
+        assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
+
+
+@pytest.mark.parametrize("L,nr,nc,ns,zc,pd,occ,tile,split", [
+    (32, 64, 6, 2, 4, 2, 4, None, 1),     # 8 slabs, the headline replica count
+    (32, 64, 6, 3, 4, 2, 4, None, 0),
+    (64, 128, 6, 2, 8, 4, 3, None, 1),    # four-word vectors
+    (40, 96, 3, 3, 8, 0, 4, None, 0),     # three word groups of one word, 5 slabs
+    (96, 64, 5, 2, 2, 0, 4, "row", 1),    # whole-row blocks, 48 slabs
+    (24, 32, 2, 2, 8, 0, 3, None, 0),     # 3 slabs: every slab depends on every slab
+    (16, 64, 6, 1, 16, 0, 3, None, 1),    # one slab
+    (32, 32, 1, 4, 16, 0, 4, None, 0),    # nc = 1, 2 slabs
+    (40, 96, 3, 3, 2, 0, 3, None, 1),
+    (96, 64, 5, 2, 4, 2, 3, "row", 0),
+])
+def test_flow_sweep_matches_oracle(L, nr, nc, ns, zc, pd, occ, tile, split):
+    ctx = _context(L, nr, ns, nc, zc, pd, occ, tile, split)
+    rng = np.random.default_rng(17 * L + nr + ns + zc)
+    st = random_state(rng, L, nr, nc, ns)
+    iters = L // 2 + 3
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(iters)
+        ctx.synchronize()  # also reports any dependency wait that timed out
+        _check(ctx, st, L, nr, nc, iters)
+
+
+@pytest.mark.parametrize("occ,split", [(3, 1), (4, 0)])
+def test_flow_sweep_frozen_sample_untouched(occ, split):
+    """micsa_set_active with the dataflow sweep: a frozen sample's tiles are
+    skipped (its counters still advance, so later tiles do not wait on it)
+    and its state stays as it was; after it is unfrozen it continues like
+    the oracle."""
+    L, nr, nc, ns = 32, 64, 4, 3
+    ctx = _context(L, nr, ns, nc, 4, 2, occ, split=split)
+    rng = np.random.default_rng(23 + occ)
+    st = random_state(rng, L, nr, nc, ns)
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(5)
+        ctx.set_active([1, 0, 1])
+        ctx.iterate(7)
+        ctx.set_active(None)
+        ctx.iterate(4)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, 16, samples=(0, 2))
+        _check(ctx, st, L, nr, nc, 9, samples=(1,))
+
+
+def test_flow_sweep_headline_shape():
+    """L=160, 2 samples x 64 replicas, nc=6 (the benchmark's shape, with its
+    whole-row blocks and 8-plane slabs), two iterations against the oracle."""
+    L, nr, nc, ns = 160, 64, 6, 2
+    ctx = _context(L, nr, ns, nc, 8, 2, 3, "row")
+    rng = np.random.default_rng(160)
+    st = random_state(rng, L, nr, nc, ns)
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(2)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, 2)
