@@ -323,13 +323,21 @@ int autotune(micsa_ctx *ctx) {
   int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, best_tma = 0;
   int best_async = 0, best_pipe = 0, best_tw = 0, best_flow = 0, n = 0;
   const int ntw = micsa_sweep_wide_differs(g.L) ? 2 : 1;
+  /* The dataflow sweep is timed only for large lattices (many slabs per
+   * half-sweep, so that its tiles rarely wait): contexts of small lattices
+   * run side by side in batches and servers, where blocks that wait on
+   * dependencies hold SM slots the other contexts' kernels need (the batched
+   * mixed-L stream lost 30% with it).  MICSA_SWEEP_FLOW=0 leaves it out
+   * everywhere. */
+  const char *ef0 = getenv("MICSA_SWEEP_FLOW");
+  const int ntm = (ef0 && !strcmp(ef0, "0")) || g.L < 128 ? 4 : 5;
   const int reps = 3;
   const int nocc = g.W % 4 ? 2 : 1; /* the 4-blocks variant exists for VW <= 2 */
   /* tm: 0 direct loads, 1 TMA-staged demon tiles, 2 cp.async double buffer (W = 2),
    * 3 loads pipelined one step ahead in registers (register budget for 3 or 2
    * blocks per SM instead of 3 or 4), 4 direct loads in one dataflow launch
    * per iteration (split: its tiles sample-major or half-sweep-major) */
-  for (int tm = 0; tm < 5; tm++)
+  for (int tm = 0; tm < ntm; tm++)
   for (int tw = 0; tw < ntw; tw++)
   for (int oc = 0; oc < nocc; oc++)
   for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
