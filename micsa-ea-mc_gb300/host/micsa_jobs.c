@@ -101,8 +101,10 @@ static int is_pow2(int64_t t) { return t > 0 && !(t & (t - 1)); }
 
 /* One shape group (same L, nr, nc, beta) in its own context and stream:
  * jobs sorted by iterations, longest first, so the running jobs are always
- * the slots [0, nrun). */
+ * the slots [0, nrun).  The context is created before any group runs (see
+ * micsa_run_batch) and destroyed by the group. */
 typedef struct {
+  micsa_ctx *ctx;
   int device, n;
   const micsa_job *jobs; /* all jobs */
   int *idx;              /* this group's jobs, longest first */
@@ -120,9 +122,8 @@ typedef struct {
 static void *run_group(void *arg) {
   group_run *gr = (group_run *)arg;
   const micsa_job *j0 = &gr->jobs[gr->idx[0]];
-  const int L = j0->L, nr = j0->nr, n = gr->n;
-  micsa_config cfg = {gr->device, L, nr, n, j0->nc};
-  micsa_ctx *ctx = NULL;
+  const int nr = j0->nr, n = gr->n;
+  micsa_ctx *ctx = gr->ctx;
   micsa_prc_t *prc = (micsa_prc_t *)malloc(sizeof(micsa_prc_t) * nr * n);
   micsa_xoshiro_t *xo = (micsa_xoshiro_t *)malloc(sizeof(micsa_xoshiro_t) * nr * n);
   int32_t *es = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * nr);
@@ -133,10 +134,6 @@ static void *run_group(void *arg) {
   if (!prc || !xo || !es || !ed || !on || !m) {
     rc = MICSA_ERR_NOMEM;
     snprintf(gr->err, sizeof gr->err, "host memory for a group of %d jobs", n);
-    goto out;
-  }
-  if ((rc = micsa_create(&cfg, &ctx))) {
-    snprintf(gr->err, sizeof gr->err, "micsa_create L=%d nr=%d n=%d failed (%d)", L, nr, n, rc);
     goto out;
   }
 #define CK(call)                                                                   \
@@ -216,6 +213,7 @@ static void *run_group(void *arg) {
 #undef CK
 out:
   micsa_destroy(ctx);
+  gr->ctx = NULL;
   free(prc), free(xo), free(es), free(ed), free(on), free(m);
   gr->rc = rc;
   return NULL;
@@ -318,9 +316,20 @@ int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spi
   }
   {
     const double t0 = now_s();
+    /* the contexts first, one after another: a shape's first context times
+     * its launch shapes, which needs the GPU to itself (timed beside the
+     * other groups' work, the choice would follow the noise) */
     for (int g = 0; g < ng; g++) {
-      grs[g] = (group_run){device, gstart[g + 1] - gstart[g], jobs, idx + gstart[g], off, maxH,
-                           maxnr, J, even, odd, prc, xo, e_spin, e_demon, MICSA_OK, {0}};
+      grs[g] = (group_run){NULL, device, gstart[g + 1] - gstart[g], jobs, idx + gstart[g], off,
+                           maxH, maxnr, J, even, odd, prc, xo, e_spin, e_demon, MICSA_OK, {0}};
+      const micsa_job *j0 = &jobs[idx[gstart[g]]];
+      micsa_config cfg = {device, j0->L, j0->nr, grs[g].n, j0->nc};
+      if ((grs[g].rc = micsa_create(&cfg, &grs[g].ctx)))
+        snprintf(grs[g].err, sizeof grs[g].err, "micsa_create L=%d nr=%d n=%d failed (%d)", j0->L,
+                 j0->nr, grs[g].n, grs[g].rc);
+    }
+    for (int g = 0; g < ng; g++) {
+      if (!grs[g].ctx) continue;
       spawned[g] = g < ng - 1 && pthread_create(&tid[g], NULL, run_group, &grs[g]) == 0;
       if (!spawned[g]) run_group(&grs[g]);
     }
