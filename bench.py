@@ -169,22 +169,25 @@ def algorithmic_bytes_per_attempt(nr):
     return (56.0 + 48.0 / nr) / 64.0
 
 
-def traffic_per_launch(L, nr, ns):
-    """DRAM bytes of one half-sweep launch from the committed ncu summary
-    (profiles/k_sweep_*.md, line 'traffic_bytes_per_launch L nr ns: N'),
-    scaled by the sites processed when only a smaller capture exists."""
+def traffic_per_launch(L, nr, ns, kernel="k_sweep"):
+    """DRAM bytes of one half-sweep of all samples from the committed ncu
+    summaries (profiles/*.md, lines 'traffic_bytes_per_launch[<kernel>] L nr
+    ns: N'; no tag = k_sweep), scaled by the sites processed when only a
+    smaller capture of that kernel exists."""
     import glob
     import re
     best = None
-    for f in glob.glob(os.path.join(ROOT, "profiles", "*.md")):
-        for m in re.finditer(r"traffic_bytes_per_launch L=(\d+) nr=(\d+) ns=(\d+): (\d+)",
+    for f in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        for m in re.finditer(r"traffic_bytes_per_launch(?:\[(\w+)\])? L=(\d+) nr=(\d+) ns=(\d+): (\d+)",
                              open(f).read()):
-            cl, cn, cs, b = (int(x) for x in m.groups())
+            if (m.group(1) or "k_sweep") != kernel:
+                continue
+            cl, cn, cs, b = (int(x) for x in m.groups()[1:])
             if (cl, cn, cs) == (L, nr, ns):
-                return float(b), "ncu capture of this shape"
+                return float(b), "ncu capture of this shape (%s)" % kernel
             if cn == nr:
                 best = (float(b) * (L ** 3 * ns) / (cl ** 3 * cs),
-                        "ncu capture at L=%d ns=%d scaled by sites" % (cl, cs))
+                        "ncu capture of %s at L=%d ns=%d scaled by sites" % (kernel, cl, cs))
     return best if best else (None, None)
 
 
@@ -252,7 +255,8 @@ def run_micsa(a, dist):
     per_launch = attempts / (2 * nc) * bpa
     achieved = per_launch / (sweep_ms * 1e-3) / 1e9
     peak, kind = peaks()
-    traffic, tnote = traffic_per_launch(L, nr, ns)
+    traffic, tnote = traffic_per_launch(L, nr, ns, "k_sweep_dep" if "load=flow" in ctx.tuning()
+                                        else "k_sweep")
     kernel = ("k_sweep_dep (dataflow sweep: the %d half-sweeps of an iteration in one launch; "
               "time per half-sweep)" % (2 * nc) if "load=flow" in ctx.tuning()
               else "k_sweep (micSA half-sweep)")
