@@ -1298,49 +1298,107 @@ k_to_ref(const micsa_geo g, const int p, const int ic, const int *__restrict__ w
 
 /* ---------------------------------------------------------- measurement */
 
+/* Per-replica counts of one lane, bit-sliced (bit r of every word belongs
+ * to replica r of the lane's 32-replica word): a carry-save accumulator of
+ * weights 1, 2, 4 and 8 (full adders as three-input LOP3s) in front of a
+ * ripple counter of sixteens, so that adding a word costs about two logic
+ * operations; one warp transpose per bit slice at the end turns the slices
+ * into counts per replica.  Capacity: 1023 per lane and replica. */
+constexpr int VC_HI = 6;
+struct vcount {
+  uint32_t ones = 0, twos = 0, fours = 0, eights = 0, hi[VC_HI] = {0, 0, 0, 0, 0, 0};
+  static __device__ __forceinline__ void half(uint32_t &acc, uint32_t a, uint32_t &c) {
+    c = acc & a;
+    acc ^= a;
+  }
+  static __device__ __forceinline__ void full(uint32_t &acc, uint32_t a, uint32_t b, uint32_t &c) {
+    c = maj3(acc, a, b);
+    acc = xor3(acc, a, b);
+  }
+  __device__ __forceinline__ void ripple(uint32_t c) {
+#pragma unroll
+    for (int k = 0; k < VC_HI; k++) {
+      const uint32_t t = hi[k] & c;
+      hi[k] ^= c;
+      c = t;
+    }
+  }
+  /* a0..a3 with weight 1, b0..b3 with weight 2 (at most 12 per call) */
+  __device__ __forceinline__ void add8(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                       uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3) {
+    uint32_t c1, c2, d1, d2, d3, e1, e2, f;
+    full(ones, a0, a1, c1);
+    full(ones, a2, a3, c2);
+    full(twos, c1, c2, d1);
+    full(twos, b0, b1, d2);
+    full(twos, b2, b3, d3);
+    full(fours, d1, d2, e1);
+    half(fours, d3, e2);
+    full(eights, e1, e2, f);
+    ripple(f);
+  }
+  /* the bits of a count c = b0 + 2 b1 + 4 b2 (at most 7 per call) */
+  __device__ __forceinline__ void add3(uint32_t b0, uint32_t b1, uint32_t b2) {
+    uint32_t c1, c2, c3, c4;
+    half(ones, b0, c1);
+    full(twos, b1, c1, c2);
+    full(fours, b2, c2, c3);
+    half(eights, c3, c4);
+    ripple(c4);
+  }
+  /* the warp's total for replica `lane` (all 32 lanes must call) */
+  __device__ __forceinline__ unsigned long long reduce(int lane) const {
+    unsigned long long t = __popc(warp_transpose32(ones, lane)) +
+                           2ull * __popc(warp_transpose32(twos, lane)) +
+                           4ull * __popc(warp_transpose32(fours, lane)) +
+                           8ull * __popc(warp_transpose32(eights, lane));
+#pragma unroll
+    for (int k = 0; k < VC_HI; k++) t += (16ull << k) * __popc(warp_transpose32(hi[k], lane));
+    return t;
+  }
+};
+
 /* Unsatisfied bonds per replica, summed over the 6 bonds of every colour-0
  * site (each bond has exactly one colour-0 end).  blockIdx.y = word w,
- * blockIdx.z = sample; warps stride over chunks of 32 sites. */
+ * blockIdx.z = sample; warps stride over chunks of 32 sites (at most 128
+ * sites per lane: the launch sizes the grid for it).  Site offsets are
+ * 32-bit (P*W < 2^32 is checked at creation). */
 __global__ void __launch_bounds__(TPB)
 k_energy(const micsa_geo g, const uint32_t *__restrict__ spin, const uint8_t *__restrict__ jb,
          unsigned long long *__restrict__ unsat) {
   const int s = blockIdx.z, w = blockIdx.y, lane = threadIdx.x & 31;
   if (micsa_frozen(g, s)) return;
-  const int L = g.L, Lh = g.Lh, W = g.W;
-  const int64_t P = g.P;
-  const uint32_t *mine = spin + (int64_t)(s * 2) * P * W + w;
-  const uint32_t *oth = spin + (int64_t)(s * 2 + 1) * P * W + w;
-  const uint8_t *jbs = jb + (int64_t)(s * 2) * P;
-  unsigned long long acc = 0;
-  const int64_t step = (int64_t)gridDim.x * TPB;
-  for (int64_t base = (int64_t)blockIdx.x * TPB + (threadIdx.x & ~31); base < P; base += step) {
-    const int64_t i = base + lane; /* P is a multiple of 32: all lanes valid */
-    const int xh = (int)(i % Lh);
-    const int64_t q = i / Lh;
-    const int y = (int)(q % L), z = (int)(q / L);
-    const int rowoff = (y + z) & 1;
-    int xe = xh + rowoff; if (xe == Lh) xe = 0;
-    int xo = xh + rowoff - 1; if (xo < 0) xo = Lh - 1;
-    const int yp = (y + 1 == L) ? 0 : y + 1, ym = (y == 0) ? L - 1 : y - 1;
-    const int zp = (z + 1 == L) ? 0 : z + 1, zm = (z == 0) ? L - 1 : z - 1;
-    const int64_t row = (int64_t)z * L;
+  const uint32_t L = g.L, Lh = g.Lh, W = g.W, P = (uint32_t)g.P;
+  const uint32_t *mine = spin + (size_t)(s * 2) * P * W + w;
+  const uint32_t *oth = spin + (size_t)(s * 2 + 1) * P * W + w;
+  const uint8_t *jbs = jb + (size_t)(s * 2) * P;
+  vcount cnt;
+  const uint32_t step = gridDim.x * TPB;
+  for (uint32_t base = blockIdx.x * TPB + (threadIdx.x & ~31u); base < P; base += step) {
+    const uint32_t i = base + lane; /* P is a multiple of 32: all lanes valid */
+    const uint32_t xh = i % Lh, q = i / Lh;
+    const uint32_t y = q % L, z = q / L;
+    const uint32_t rowoff = (y + z) & 1;
+    uint32_t xe = xh + rowoff; if (xe == Lh) xe = 0;
+    const uint32_t xo = (xh + rowoff == 0) ? Lh - 1 : xh + rowoff - 1;
+    const uint32_t yp = (y + 1 == L) ? 0 : y + 1, ym = (y == 0) ? L - 1 : y - 1;
+    const uint32_t zp = (z + 1 == L) ? 0 : z + 1, zm = (z == 0) ? L - 1 : z - 1;
+    const uint32_t row = z * L;
     const uint32_t sw = __ldg(mine + i * W);
     const uint32_t jbits = __ldg(jbs + i);
     const uint32_t f0 = sw ^ __ldg(oth + ((row + y) * Lh + xe) * W) ^ jmask(jbits, 0);
     const uint32_t f1 = sw ^ __ldg(oth + ((row + yp) * Lh + xh) * W) ^ jmask(jbits, 1);
-    const uint32_t f2 = sw ^ __ldg(oth + (((int64_t)zp * L + y) * Lh + xh) * W) ^ jmask(jbits, 2);
+    const uint32_t f2 = sw ^ __ldg(oth + ((zp * L + y) * Lh + xh) * W) ^ jmask(jbits, 2);
     const uint32_t f3 = sw ^ __ldg(oth + ((row + y) * Lh + xo) * W) ^ jmask(jbits, 3);
     const uint32_t f4 = sw ^ __ldg(oth + ((row + ym) * Lh + xh) * W) ^ jmask(jbits, 4);
-    const uint32_t f5 = sw ^ __ldg(oth + (((int64_t)zm * L + y) * Lh + xh) * W) ^ jmask(jbits, 5);
+    const uint32_t f5 = sw ^ __ldg(oth + ((zm * L + y) * Lh + xh) * W) ^ jmask(jbits, 5);
     /* bit-sliced sum of six bits: c = b0 + 2 b1 + 4 b2 */
-    const uint32_t sa = f0 ^ f1 ^ f2, ca = (f0 & f1) | (f2 & (f0 ^ f1));
-    const uint32_t sb = f3 ^ f4 ^ f5, cb = (f3 & f4) | (f5 & (f3 ^ f4));
+    const uint32_t sa = xor3(f0, f1, f2), ca = maj3(f0, f1, f2);
+    const uint32_t sb = xor3(f3, f4, f5), cb = maj3(f3, f4, f5);
     const uint32_t b0 = sa ^ sb, c0 = sa & sb;
-    const uint32_t b1 = ca ^ cb ^ c0, b2 = (ca & cb) | (c0 & (ca ^ cb));
-    acc += __popc(warp_transpose32(b0, lane)) + 2u * __popc(warp_transpose32(b1, lane)) +
-           4u * __popc(warp_transpose32(b2, lane));
+    cnt.add3(b0, xor3(ca, cb, c0), maj3(ca, cb, c0));
   }
-  atomicAdd(unsat + (int64_t)s * g.nr + w * 32 + lane, acc);
+  atomicAdd(unsat + (int64_t)s * g.nr + w * 32 + lane, cnt.reduce(lane));
 }
 
 /* Demon energy per replica: blockIdx.y = (plane pi = p*nc + ic)*W + w. */
@@ -1362,31 +1420,41 @@ k_demon_energy(const micsa_geo g, const uint32_t *__restrict__ d0, const uint32_
 }
 
 /* Demon energy with 16-byte loads, for W in {1, 2, 4}: a plane (sample s,
- * plane pi) is P*W consecutive words; component c of a lane's 4-word vector
- * at word 4k is word w = c % W of its site (4 % W == 0), the same for every
- * lane, so one transpose per component gives lane l the count of replica
- * w*32 + l.  blockIdx.y = s*2*nc + pi; blocks stride over the plane. */
+ * plane pi) is P*W consecutive words; component c of a 4-word vector at
+ * word 4k is word w = c % W of its site (4 % W == 0).  A lane loads four
+ * vectors of each demon array per trip (lane-contiguous, 512 bytes per warp
+ * and load) and adds component c's words into the bit-sliced counter of
+ * word c % W, D0 with weight 1 and D1 with weight 2; the counters are
+ * transposed into per-replica counts once, at the end.  At most 16 trips
+ * per lane (the launch sizes the grid for it) keep every counter within its
+ * capacity.  blockIdx.y = s*2*nc + pi; blocks stride over the plane. */
+template <int W>
 __global__ void __launch_bounds__(TPB)
-k_demon_energy_v4(const micsa_geo g, const uint32_t *__restrict__ d0,
+k_demon_energy_cs(const micsa_geo g, const uint32_t *__restrict__ d0,
                   const uint32_t *__restrict__ d1, unsigned long long *__restrict__ dem) {
   const int plane = blockIdx.y, s = plane / (2 * g.nc), lane = threadIdx.x & 31;
   if (micsa_frozen(g, s)) return;
-  const int64_t nvec = g.P * g.W / 4; /* P is a multiple of 32 */
-  const uint4 *a = (const uint4 *)(d0 + (int64_t)plane * g.P * g.W);
-  const uint4 *b = (const uint4 *)(d1 + (int64_t)plane * g.P * g.W);
-  unsigned long long acc[4] = {0, 0, 0, 0};
-  const int64_t step = (int64_t)gridDim.x * TPB;
-  for (int64_t base = (int64_t)blockIdx.x * TPB + (threadIdx.x & ~31); base < nvec; base += step) {
-    const int64_t i = base + lane; /* nvec is a multiple of 32: whole warps */
-    const uint4 x = __ldcs(a + i), y = __ldcs(b + i);
-    acc[0] += __popc(warp_transpose32(x.x, lane)) + 2u * __popc(warp_transpose32(y.x, lane));
-    acc[1] += __popc(warp_transpose32(x.y, lane)) + 2u * __popc(warp_transpose32(y.y, lane));
-    acc[2] += __popc(warp_transpose32(x.z, lane)) + 2u * __popc(warp_transpose32(y.z, lane));
-    acc[3] += __popc(warp_transpose32(x.w, lane)) + 2u * __popc(warp_transpose32(y.w, lane));
+  const uint32_t nvec = (uint32_t)(g.P * W / 4);
+  const uint4 *a = (const uint4 *)(d0 + (int64_t)plane * g.P * W);
+  const uint4 *b = (const uint4 *)(d1 + (int64_t)plane * g.P * W);
+  vcount cnt[W];
+  const uint32_t stride = gridDim.x * TPB * 4;
+  for (uint32_t v0 = (blockIdx.x * TPB + (threadIdx.x & ~31u)) * 4; v0 < nvec; v0 += stride) {
+    uint4 x[4], y[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const uint32_t v = v0 + k * 32 + lane;
+      x[k] = v < nvec ? __ldcs(a + v) : make_uint4(0, 0, 0, 0);
+      y[k] = v < nvec ? __ldcs(b + v) : make_uint4(0, 0, 0, 0);
+    }
+    cnt[0].add8(x[0].x, x[1].x, x[2].x, x[3].x, y[0].x, y[1].x, y[2].x, y[3].x);
+    cnt[1 % W].add8(x[0].y, x[1].y, x[2].y, x[3].y, y[0].y, y[1].y, y[2].y, y[3].y);
+    cnt[2 % W].add8(x[0].z, x[1].z, x[2].z, x[3].z, y[0].z, y[1].z, y[2].z, y[3].z);
+    cnt[3 % W].add8(x[0].w, x[1].w, x[2].w, x[3].w, y[0].w, y[1].w, y[2].w, y[3].w);
   }
-  for (int c = g.W; c < 4; c++) acc[c % g.W] += acc[c]; /* component c is word c % W */
   unsigned long long *out = dem + (int64_t)s * g.nr + lane;
-  for (int w = 0; w < g.W; w++) atomicAdd(out + w * 32, acc[w]);
+#pragma unroll
+  for (int w = 0; w < W; w++) atomicAdd(out + w * 32, cnt[w].reduce(lane));
 }
 
 /* Overlap and C4 of the replica pairs (2k, 2k+1): with t = s(x) ^ s(x'),
@@ -1705,7 +1773,11 @@ static int measure_blocks(int64_t sites, int64_t slices) {
 
 cudaError_t micsa_launch_energy(const micsa_geo &g, const uint32_t *spin, const uint8_t *jb,
                                 unsigned long long *unsat, cudaStream_t st) {
-  dim3 grid(measure_blocks(g.P, (int64_t)g.W * g.ns), g.W, g.ns);
+  /* at most 128 sites per lane: the counters hold 1023 per replica */
+  int bx = measure_blocks(g.P, (int64_t)g.W * g.ns);
+  const int64_t need = (g.P + (int64_t)TPB * 128 - 1) / ((int64_t)TPB * 128);
+  if (bx < need) bx = (int)need;
+  dim3 grid(bx, g.W, g.ns);
   k_energy<<<grid, TPB, 0, st>>>(g, spin, jb, unsat);
   return cudaGetLastError();
 }
@@ -1713,10 +1785,13 @@ cudaError_t micsa_launch_energy(const micsa_geo &g, const uint32_t *spin, const 
 cudaError_t micsa_launch_demon_energy(const micsa_geo &g, const uint32_t *d0, const uint32_t *d1,
                                       unsigned long long *dem, cudaStream_t st) {
   if (g.W == 1 || g.W == 2 || g.W == 4) {
-    const int64_t planes = (int64_t)2 * g.nc * g.ns, vec_blocks = (g.P * g.W / 4 + TPB - 1) / TPB;
-    int64_t bx = (8 * 152 + planes - 1) / planes; /* about 8 blocks per SM in all */
-    if (bx > vec_blocks) bx = vec_blocks;
-    k_demon_energy_v4<<<dim3((unsigned)(bx < 1 ? 1 : bx), (unsigned)planes), TPB, 0, st>>>(g, d0, d1, dem);
+    /* at most 16 trips of 4 vectors per lane (counter capacity) */
+    const int64_t planes = (int64_t)2 * g.nc * g.ns, nvec = g.P * g.W / 4;
+    const int64_t bx = (nvec + (int64_t)TPB * 4 * 16 - 1) / ((int64_t)TPB * 4 * 16);
+    const dim3 grid((unsigned)(bx < 1 ? 1 : bx), (unsigned)planes);
+    if (g.W == 1) k_demon_energy_cs<1><<<grid, TPB, 0, st>>>(g, d0, d1, dem);
+    else if (g.W == 2) k_demon_energy_cs<2><<<grid, TPB, 0, st>>>(g, d0, d1, dem);
+    else k_demon_energy_cs<4><<<grid, TPB, 0, st>>>(g, d0, d1, dem);
     return cudaGetLastError();
   }
   dim3 grid(measure_blocks(g.P, (int64_t)2 * g.nc * g.W * g.ns), 2 * g.nc * g.W, g.ns);
