@@ -1358,6 +1358,23 @@ struct vcount {
   }
 };
 
+/* Adds v (lane l: the warp's total for replica l) of every warp of the block
+ * into out[l]: one atomic per lane and block instead of one per warp.  All
+ * threads of the block must call; buf holds TPB/32 * 32 entries. */
+__device__ __forceinline__ void block_add(unsigned long long v, unsigned long long *buf,
+                                          unsigned long long *out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  buf[warp * 32 + lane] = v;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long t = 0;
+#pragma unroll
+    for (int k = 0; k < TPB / 32; k++) t += buf[k * 32 + lane];
+    atomicAdd(out + lane, t);
+  }
+  __syncthreads();
+}
+
 /* Unsatisfied bonds per replica, summed over the 6 bonds of every colour-0
  * site (each bond has exactly one colour-0 end).  blockIdx.y = word w,
  * blockIdx.z = sample; warps stride over chunks of 32 sites (at most 128
@@ -1366,6 +1383,7 @@ struct vcount {
 __global__ void __launch_bounds__(TPB)
 k_energy(const micsa_geo g, const uint32_t *__restrict__ spin, const uint8_t *__restrict__ jb,
          unsigned long long *__restrict__ unsat) {
+  __shared__ unsigned long long buf[TPB];
   const int s = blockIdx.z, w = blockIdx.y, lane = threadIdx.x & 31;
   if (micsa_frozen(g, s)) return;
   const uint32_t L = g.L, Lh = g.Lh, W = g.W, P = (uint32_t)g.P;
@@ -1398,7 +1416,7 @@ k_energy(const micsa_geo g, const uint32_t *__restrict__ spin, const uint8_t *__
     const uint32_t b0 = sa ^ sb, c0 = sa & sb;
     cnt.add3(b0, xor3(ca, cb, c0), maj3(ca, cb, c0));
   }
-  atomicAdd(unsat + (int64_t)s * g.nr + w * 32 + lane, cnt.reduce(lane));
+  block_add(cnt.reduce(lane), buf, unsat + (int64_t)s * g.nr + w * 32);
 }
 
 /* Demon energy per replica: blockIdx.y = (plane pi = p*nc + ic)*W + w. */
@@ -1432,6 +1450,7 @@ template <int W>
 __global__ void __launch_bounds__(TPB)
 k_demon_energy_cs(const micsa_geo g, const uint32_t *__restrict__ d0,
                   const uint32_t *__restrict__ d1, unsigned long long *__restrict__ dem) {
+  __shared__ unsigned long long buf[TPB];
   const int plane = blockIdx.y, s = plane / (2 * g.nc), lane = threadIdx.x & 31;
   if (micsa_frozen(g, s)) return;
   const uint32_t nvec = (uint32_t)(g.P * W / 4);
@@ -1452,9 +1471,8 @@ k_demon_energy_cs(const micsa_geo g, const uint32_t *__restrict__ d0,
     cnt[2 % W].add8(x[0].z, x[1].z, x[2].z, x[3].z, y[0].z, y[1].z, y[2].z, y[3].z);
     cnt[3 % W].add8(x[0].w, x[1].w, x[2].w, x[3].w, y[0].w, y[1].w, y[2].w, y[3].w);
   }
-  unsigned long long *out = dem + (int64_t)s * g.nr + lane;
 #pragma unroll
-  for (int w = 0; w < W; w++) atomicAdd(out + w * 32, cnt[w].reduce(lane));
+  for (int w = 0; w < W; w++) block_add(cnt[w].reduce(lane), buf, dem + (int64_t)s * g.nr + w * 32);
 }
 
 /* Overlap and C4 of the replica pairs (2k, 2k+1): with t = s(x) ^ s(x'),
