@@ -163,20 +163,20 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
  * pipe: each z step's loads issued one step ahead into registers |
  * flow: the iteration's half-sweeps in one dataflow launch, one block per
  * tile, ordered by per-slab dependency counters; split then orders its
- * tiles sample-major (1) or half-sweep-major (0)>
+ * tiles sample-major (1) or half-sweep-major (0) | quad: direct loads with
+ * four one-word sites per thread (32 replicas)>
  * tile=<default | row: blocks span whole rows along x> |
- * <zc>/<pd>/<split>/<occ>/<load 0|1|2|3|4>/<tile 0|1>:<ms per half-sweep> ...",
+ * <zc>/<pd>/<split>/<occ>/<load 0|1|2|3|4|5>/<tile 0|1>:<ms per half-sweep> ...",
  * with " cached" before the "|" when the choice and its table were taken
  * over from an earlier context of the same device, L, nr, samples and nc in
  * this process (MICSA_TUNE_CACHE=0 times every context instead).  The
  * environment variables MICSA_SWEEP_ZC, MICSA_SWEEP_PD, MICSA_SWEEP_SPLIT,
  * MICSA_SWEEP_OCC, MICSA_SWEEP_TMA, MICSA_SWEEP_ASYNC, MICSA_SWEEP_PIPE,
- * MICSA_SWEEP_FLOW and MICSA_SWEEP_TILE (=row), read by micsa_create, pin
- * the shape and skip the timing (no candidates listed then).  The dataflow
- * sweep is timed for L >= 128 only; MICSA_SWEEP_FLOW=0 alone leaves it out
- * everywhere.
- * The reference has fixed launch geometry (calculate_blocks,
- * ini.c:580-602). */
+ * MICSA_SWEEP_FLOW, MICSA_SWEEP_QUAD and MICSA_SWEEP_TILE (=row), read by
+ * micsa_create, pin the shape and skip the timing (no candidates listed
+ * then).  The dataflow sweep is timed for L >= 128 only; MICSA_SWEEP_FLOW=0
+ * alone leaves it out everywhere.  The reference has fixed launch geometry
+ * (calculate_blocks, ini.c:580-602). */
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n);
 
 /* Spin energies computed without allocating any device memory; this entry

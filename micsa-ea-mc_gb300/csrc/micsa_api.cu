@@ -232,7 +232,7 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
  * choice and table instead of timing again, so batches and servers that open
  * many contexts of a few shapes pay for each shape once. */
 struct tune_entry {
-  int zc, pd, split, occ, tma, async, pipe, tw, flow, n;
+  int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, n;
   std::vector<int> zcs, pds, splits, occs, tmas, tws;
   std::vector<double> ms;
 };
@@ -274,13 +274,14 @@ int autotune(micsa_ctx *ctx) {
     const char *es = getenv("MICSA_SWEEP_SPLIT"), *eo = getenv("MICSA_SWEEP_OCC"),
                *et = getenv("MICSA_SWEEP_TMA"), *ea = getenv("MICSA_SWEEP_ASYNC"),
                *ep2 = getenv("MICSA_SWEEP_PIPE"), *ew = getenv("MICSA_SWEEP_TILE"),
-               *ef = getenv("MICSA_SWEEP_FLOW");
+               *ef = getenv("MICSA_SWEEP_FLOW"), *eq = getenv("MICSA_SWEEP_QUAD");
     ctx->split = es && atoi(es) && g.ns > 1;
     g.tma = et && atoi(et) && ctx->tma.ok;
     g.async = ea && atoi(ea) && g.W == 2 && !g.tma;
     g.pipe = ep2 && atoi(ep2) && !g.tma && !g.async;
-    g.tw = ew && !strcmp(ew, "row") && !g.tma && micsa_sweep_wide_differs(g.L);
+    g.tw = ew && !strcmp(ew, "row") && !g.tma && micsa_sweep_wide_differs(g.L, eq && atoi(eq) ? 4 : 2);
     g.flow = ef && atoi(ef) && !g.tma && !g.async && !g.pipe;
+    g.quad = eq && atoi(eq) && g.W == 1 && !g.tma && !g.async && !g.pipe && !g.flow;
     const int oc = eo ? atoi(eo) : 3;
     g.occ = g.pipe ? (oc == 2 ? 2 : 3) : (oc == 4 ? 4 : 3);
     ctx->ntune = 0;
@@ -302,6 +303,7 @@ int autotune(micsa_ctx *ctx) {
       g.pipe = t.pipe;
       g.tw = t.tw;
       g.flow = t.flow;
+      g.quad = t.quad;
       ctx->ntune = t.n;
       for (int c = 0; c < t.n; c++) {
         ctx->tune_zc[c] = t.zcs[c];
@@ -321,8 +323,8 @@ int autotune(micsa_ctx *ctx) {
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
   int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, best_tma = 0;
-  int best_async = 0, best_pipe = 0, best_tw = 0, best_flow = 0, n = 0;
-  const int ntw = micsa_sweep_wide_differs(g.L) ? 2 : 1;
+  int best_async = 0, best_pipe = 0, best_tw = 0, best_flow = 0, best_quad = 0, n = 0;
+  const int ntw = micsa_sweep_wide_differs(g.L) ? 2 : 1, ntw4 = micsa_sweep_wide_differs(g.L, 4) ? 2 : 1;
   /* The dataflow sweep is timed only for large lattices (many slabs per
    * half-sweep, so that its tiles rarely wait): contexts of small lattices
    * run side by side in batches and servers, where blocks that wait on
@@ -330,15 +332,16 @@ int autotune(micsa_ctx *ctx) {
    * mixed-L stream lost 30% with it).  MICSA_SWEEP_FLOW=0 leaves it out
    * everywhere. */
   const char *ef0 = getenv("MICSA_SWEEP_FLOW");
-  const int ntm = (ef0 && !strcmp(ef0, "0")) || g.L < 128 ? 4 : 5;
+  const bool try_flow = !(ef0 && !strcmp(ef0, "0")) && g.L >= 128;
   const int reps = 3;
   const int nocc = g.W % 4 ? 2 : 1; /* the 4-blocks variant exists for VW <= 2 */
   /* tm: 0 direct loads, 1 TMA-staged demon tiles, 2 cp.async double buffer (W = 2),
    * 3 loads pipelined one step ahead in registers (register budget for 3 or 2
    * blocks per SM instead of 3 or 4), 4 direct loads in one dataflow launch
-   * per iteration (split: its tiles sample-major or half-sweep-major) */
-  for (int tm = 0; tm < ntm; tm++)
-  for (int tw = 0; tw < ntw; tw++)
+   * per iteration (split: its tiles sample-major or half-sweep-major), 5
+   * direct loads with four one-word sites per thread (W = 1) */
+  for (int tm = 0; tm < 6; tm++)
+  for (int tw = 0; tw < (tm == 5 ? ntw4 : ntw); tw++)
   for (int oc = 0; oc < nocc; oc++)
   for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
   for (int c = 0; c < nz; c++)
@@ -347,6 +350,7 @@ int autotune(micsa_ctx *ctx) {
       if (tm == 1 && (!ctx->tma.ok || zcs[c] > 4)) continue; /* staged tiles: <= 4 planes */
       if (tm == 2 && (g.W != 2 || pds[d])) continue;          /* no L2 prefetch there */
       if (tw && (tm == 1 || tm == 2)) continue; /* whole-row blocks: direct and pipelined loads */
+      if ((tm == 4 && !try_flow) || (tm == 5 && g.W != 1)) continue;
       g.zc = zcs[c];
       g.pd = pds[d];
       g.occ = tm == 3 ? (oc ? 2 : 3) : (oc ? 4 : 3);
@@ -355,6 +359,7 @@ int autotune(micsa_ctx *ctx) {
       g.pipe = tm == 3;
       g.tw = tw;
       g.flow = tm == 4;
+      g.quad = tm == 5;
       /* one iteration's half-sweeps in their launch order, captured and
        * replayed as a graph the way micsa_iterate runs them: timed launch by
        * launch, small lattices would measure the host's launch rate */
@@ -402,6 +407,7 @@ int autotune(micsa_ctx *ctx) {
         best_pipe = g.pipe;
         best_tw = g.tw;
         best_flow = g.flow;
+        best_quad = g.quad;
       }
     }
   ctx->ntune = n;
@@ -414,6 +420,7 @@ int autotune(micsa_ctx *ctx) {
   g.pipe = best_pipe;
   g.tw = best_tw;
   g.flow = best_flow;
+  g.quad = best_quad;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (use_cache) {
@@ -427,6 +434,7 @@ int autotune(micsa_ctx *ctx) {
     t.pipe = g.pipe;
     t.tw = g.tw;
     t.flow = g.flow;
+    t.quad = g.quad;
     t.n = n;
     t.zcs.assign(ctx->tune_zc, ctx->tune_zc + n);
     t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
@@ -491,6 +499,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.pipe = 0;
   g.tw = 0;
   g.flow = 0;
+  g.quad = 0;
   {
     /* MICSA_PDL=0: plain launches of the sweeps */
     const char *e = getenv("MICSA_PDL");
@@ -573,7 +582,7 @@ int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
   int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s%s |", ctx->g.zc,
                    ctx->g.pd, ctx->split, ctx->g.occ,
-                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : (ctx->g.flow ? "flow" : "direct"))),
+                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : (ctx->g.flow ? "flow" : (ctx->g.quad ? "quad" : "direct")))),
                    ctx->g.tw ? "row" : "default", ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
     k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],

@@ -340,6 +340,38 @@ template <int VW, bool WIDE> struct pairs {
   }
 };
 
+/* Four sites of one word each (one word group, W = 1): their words are
+ * adjacent and move as one 16-byte vector. */
+struct quads {
+  static __device__ __forceinline__ void ld_nc(const uint32_t *a, uint32_t, uint32_t (&o)[4], uint64_t p) { hint<4>::ld_nc(a, o, p); }
+  static __device__ __forceinline__ void ld_co(const uint32_t *a, uint32_t, uint32_t (&o)[4], uint64_t p) { hint<4>::ld_co(a, o, p); }
+  static __device__ __forceinline__ void ld(const uint32_t *a, uint32_t, uint32_t (&o)[4], uint64_t p) { hint<4>::ld(a, o, p); }
+  static __device__ __forceinline__ void ld_na(const uint32_t *a, uint32_t, uint32_t (&o)[4], uint64_t p) { hint<4>::ld_na(a, o, p); }
+  static __device__ __forceinline__ void st(uint32_t *a, uint32_t, const uint32_t (&o)[4], uint64_t p) { hint<4>::st(a, o, p); }
+  template <bool FLOW>
+  static __device__ __forceinline__ void ld_oth(const uint32_t *a, uint32_t W, uint32_t (&o)[4], uint64_t p) {
+    if (FLOW) ld_co(a, W, o, p); else ld_nc(a, W, o, p);
+  }
+};
+/* the loader of S sites x VW words: pairs (S = 2) or quads (S = 4, VW = 1) */
+template <int VW, bool WIDE, int S> struct sites_io { using type = pairs<VW, WIDE>; };
+template <> struct sites_io<1, true, 4> { using type = quads; };
+
+__device__ __forceinline__ uint32_t ld_u32_keep(const uint8_t *a, uint64_t pol) {
+  uint32_t v;
+  asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_na_u32(const uint32_t *a, uint64_t pol) {
+  uint32_t o[1];
+  hint<1>::ld_na(a, o, pol);
+  return o[0];
+}
+__device__ __forceinline__ void st_u32(uint32_t *a, uint32_t v, uint64_t pol) {
+  const uint32_t o[1] = {v};
+  hint<1>::st(a, o, pol);
+}
+
 /* Half-sweep of colour p.  One thread owns two adjacent columns (x/2 = 2j,
  * 2j+1; y) of one sample, VW replica words each (group grp of G = W/VW), and
  * marches over the z chunk [z0, z0 + zc).  The two sites share their row
@@ -349,30 +381,34 @@ template <int VW, bool WIDE> struct pairs {
  * extra other-colour word for the remaining x-neighbour, the two coupling
  * bytes and the two demon words per plane.  Block = (TX pairs along x/2) x
  * (TY rows); TX divides L/4; grid = (L/4/TX, ytiles*ns*G, L/zc).
+ * With S = 4 (one word per site, W = 1) a thread owns four adjacent columns
+ * (x/2 = 4j .. 4j+3) instead of two, and every load moves 16 bytes, as a
+ * pair of 64-replica sites does: TX divides L/8.
  * In-plane offsets are 32-bit (P*W < 2^32 is checked at creation). */
 /* One block's tile of a half-sweep: sample s, word group grp, row tile
  * `tile`, x block bx, z planes [z0, z0 + zc), demon walk kwalk.  FLOW: the
  * other colour is read through the coherent path (other tiles of the same
  * dataflow launch write it). */
-template <int VW, bool MICSA, bool WIDE, bool TMA, bool FLOW>
+template <int VW, bool MICSA, bool WIDE, bool TMA, bool FLOW, int S = 2>
 __device__ __forceinline__ void sweep_block(
     const micsa_geo &g, const int p, const int ic, const uint32_t s, const uint32_t grp,
     const uint32_t tile, const uint32_t bx, const uint32_t z0, const int zc, const int pd,
     const int kwalk, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
     uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb, const uint32_t *__restrict__ rnd,
     const micsa_tma &tm) {
-  constexpr int N = 2 * VW; /* words per pair */
-  using PR = pairs<VW, WIDE>;
+  static_assert(S == 2 || (S == 4 && VW == 1 && WIDE && !TMA), "four sites: one word each");
+  constexpr int N = S * VW; /* words per thread and plane */
+  using PR = typename sites_io<VW, WIDE, S>::type;
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
   const uint32_t y = tile * blockDim.y + threadIdx.y;
   if (y >= L) return;
-  const uint32_t xa = 2 * (bx * blockDim.x + threadIdx.x); /* x/2 of site A */
+  const uint32_t xa = S * (bx * blockDim.x + threadIdx.x); /* x/2 of the first site */
   const uint32_t plane = L * Lh;
   const uint32_t row = y * Lh + xa;
   const uint32_t rowN = (y + 1 == L) ? xa : row + Lh;
   const uint32_t rowS = (y == 0) ? row + (L - 1) * Lh : row - Lh;
-  const uint32_t rowXp = (xa + 2 == Lh) ? row + 2 - Lh : row + 2; /* x/2 = 2j+2 */
-  const uint32_t rowXm = (xa == 0) ? row + Lh - 1 : row - 1;      /* x/2 = 2j-1 */
+  const uint32_t rowXp = (xa + S == Lh) ? row + S - Lh : row + S; /* x/2 = xa+S */
+  const uint32_t rowXm = (xa == 0) ? row + Lh - 1 : row - 1;      /* x/2 = xa-1 */
   const size_t P = (size_t)g.P;
   uint32_t *mine = spin + (size_t)(s * 2 + p) * P * W + grp * VW;
   const uint32_t *oth = spin + (size_t)(s * 2 + (p ^ 1)) * P * W + grp * VW;
@@ -381,7 +417,9 @@ __device__ __forceinline__ void sweep_block(
 
   /* demon plane (p, ic): the demon of site x sits at x - sgn*2k*e_axis after
    * k walks (see micsa_kernels.cuh).  An x shift by an odd number of x/2
-   * steps separates the pair's two demon words (and may wrap between them). */
+   * steps separates the pair's two demon words (and may wrap between them);
+   * with four sites, any shift that is not a multiple of 4 x/2 steps makes
+   * the four words separate loads. */
   uint32_t *q0b = nullptr, *q1b = nullptr;
   uint32_t drowA = row, drowB = row + 1, zd = z0;
   bool dpair = true;
@@ -395,7 +433,7 @@ __device__ __forceinline__ void sweep_block(
       const int xe = (xd + 1 == (int)Lh) ? 0 : xd + 1;
       drowA = y * Lh + (uint32_t)xd;
       drowB = y * Lh + (uint32_t)xe;
-      dpair = !(sh & 1);
+      dpair = !(sh & (S - 1));
     } else if (axis == 1) {
       int yd = (int)y - 2 * sh;
       yd += yd < 0 ? (int)L : (yd >= (int)L ? -(int)L : 0);
@@ -476,7 +514,7 @@ __device__ __forceinline__ void sweep_block(
       hint<VW>::ld_co(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
     else
       hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
-    const uint32_t jb2 = ld_u16_keep(jbp + zo + row, keep);
+    const uint32_t jbs = S == 4 ? ld_u32_keep(jbp + zo + row, keep) : ld_u16_keep(jbp + zo + row, keep);
     bool from_smem = false;
     if (TMA && staged) {
       if (mbar_wait(bars + t, 0)) {
@@ -500,6 +538,15 @@ __device__ __forceinline__ void sweep_block(
         if (dpair) {
           PR::ld_na(q0b + sa, W, a0, strm);
           PR::ld_na(q1b + sa, W, a1, strm);
+        } else if (S == 4) { /* four single words, each wrapped along the row */
+          const uint32_t xd = drowA % Lh, rbase = zdd * plane + (drowA - xd);
+#pragma unroll
+          for (int k = 0; k < N; k++) {
+            uint32_t xk = xd + k;
+            xk -= xk >= Lh ? Lh : 0;
+            a0[k] = ld_na_u32(q0b + rbase + xk, strm);
+            a1[k] = ld_na_u32(q1b + rbase + xk, strm);
+          }
         } else {
           const uint32_t sb = (zdd * plane + drowB) * W;
           uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
@@ -526,21 +573,31 @@ __device__ __forceinline__ void sweep_block(
       PR::ld_na(rb + P * W, W, a1, strm);
       PR::ld_na(rb + 2 * P * W, W, a2, strm);
     }
-    /* x-neighbours: site A (x/2 = 2j) and B (2j+1) of colour p see, in the
-     * other colour, +x at x/2 + rowoff and -x at x/2 + rowoff - 1 */
+    /* x-neighbours: the thread's site k (x/2 = xa + k) of colour p sees, in
+     * the other colour, +x at x/2 + rowoff and -x at x/2 + rowoff - 1: words
+     * of v0, or ext past either end */
 #pragma unroll
-    for (int site = 0; site < 2; site++) {
-      const uint32_t jb6 = (jb2 >> (8 * site)) & 0xffu;
+    for (int site = 0; site < S; site++) {
+      const uint32_t jb6 = (jbs >> (8 * site)) & 0xffu;
       const uint32_t mE = jmask(jb6, 0), mN = jmask(jb6, 1), mU = jmask(jb6, 2);
       const uint32_t mO = jmask(jb6, 3), mS = jmask(jb6, 4), mD = jmask(jb6, 5);
 #pragma unroll
       for (int w = 0; w < VW; w++) {
         const int o = site * VW + w;
-        /* A: +x = rowoff ? v0[B] : v0[A], -x = rowoff ? v0[A] : ext
-         * B: +x = rowoff ? ext : v0[B],   -x = rowoff ? v0[B] : v0[A] */
-        const uint32_t cA = v0[w], cB = v0[VW + w], ex = ext[w];
-        const uint32_t nE = site == 0 ? (rowoff ? cB : cA) : (rowoff ? ex : cB);
-        const uint32_t nO = site == 0 ? (rowoff ? cA : ex) : (rowoff ? cB : cA);
+        /* site k: +x = rowoff ? (k+1 < S ? v0[k+1] : ext) : v0[k],
+         *         -x = rowoff ? v0[k] : (k > 0 ? v0[k-1] : ext) */
+        uint32_t nE, nO;
+        if constexpr (S == 2) { /* A = site 0, B = site 1 */
+          const uint32_t cA = v0[w], cB = v0[VW + w], ex = ext[w];
+          nE = site == 0 ? (rowoff ? cB : cA) : (rowoff ? ex : cB);
+          nO = site == 0 ? (rowoff ? cA : ex) : (rowoff ? cB : cA);
+        } else {
+          const uint32_t ck = v0[o], ex = ext[w];
+          const uint32_t cn = site + 1 < S ? v0[(site + 1 < S ? site + 1 : 0) * VW + w] : ex;
+          const uint32_t cp = site > 0 ? v0[(site > 0 ? site - 1 : 0) * VW + w] : ex;
+          nE = rowoff ? cn : ck;
+          nO = rowoff ? ck : cp;
+        }
         const uint32_t sw = own[o];
         const uint32_t f0 = xor3(sw, nE, mE), f1 = xor3(sw, vn[o], mN), f2 = xor3(sw, up[o], mU);
         const uint32_t f3 = xor3(sw, nO, mO), f4 = xor3(sw, vs[o], mS), f5 = xor3(sw, vm[o], mD);
@@ -560,6 +617,15 @@ __device__ __forceinline__ void sweep_block(
       if (dpair) {
         PR::st(q0b + sa, W, a0, strm);
         PR::st(q1b + sa, W, a1, strm);
+      } else if (S == 4) {
+        const uint32_t xd = drowA % Lh, rbase = zdd * plane + (drowA - xd);
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+          uint32_t xk = xd + k;
+          xk -= xk >= Lh ? Lh : 0;
+          st_u32(q0b + rbase + xk, a0[k], strm);
+          st_u32(q1b + rbase + xk, a1[k], strm);
+        }
       } else {
         const uint32_t sb = (zdd * plane + drowB) * W;
         uint32_t x0[VW], x1[VW], y0[VW], y1[VW];
@@ -583,7 +649,7 @@ __device__ __forceinline__ void sweep_block(
   }
 }
 
-template <int VW, bool MICSA, bool WIDE, int MINB, bool TMA>
+template <int VW, bool MICSA, bool WIDE, int MINB, bool TMA, int S = 2>
 __global__ void __launch_bounds__(TPB, MINB)
 k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const int G,
         const int zc, const int pd, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
@@ -597,8 +663,8 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
   /* the walk and the run flag are loaded together: one round trip */
   const int kwalk = MICSA ? __ldg(walk + s) : 0;
   if (micsa_frozen(g, (int)s)) return;
-  sweep_block<VW, MICSA, WIDE, TMA, false>(g, p, ic, s, grp, tile, blockIdx.x, blockIdx.z * zc, zc,
-                                           pd, kwalk, spin, d0, d1, jb, rnd, tm);
+  sweep_block<VW, MICSA, WIDE, TMA, false, S>(g, p, ic, s, grp, tile, blockIdx.x, blockIdx.z * zc,
+                                              zc, pd, kwalk, spin, d0, d1, jb, rnd, tm);
 }
 
 /* ---------------------------------------------------- dataflow sweep */
@@ -1553,10 +1619,11 @@ inline int blocks_for(int64_t n, int per_block) {
  * rows (wide, when L/4 is not already that and fits a block): a row's demon
  * words are then read as one run, so the x translation of the demon walk
  * shifts one run instead of misaligning several short ones. */
-static void sweep_tile(int L, int wide, int *tx, int *ty) {
+static void sweep_tile(int L, int wide, int *tx, int *ty, int S = 2) {
+  const int cols = L / 2 / S; /* threads a row needs */
   int x = 32;
-  while ((L / 4) % x) x >>= 1;
-  if (wide && L / 4 <= TPB / 2) x = L / 4;
+  while (cols % x) x >>= 1;
+  if (wide && cols <= TPB / 2) x = cols;
   *tx = x;
   *ty = TPB / x;
 }
@@ -1613,6 +1680,20 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
   }
   micsa_tma none;
   const micsa_tma &t = tm ? *tm : none;
+  if constexpr (VW == 1) {
+    if (micsa && g.quad && G == 1 && !tma) { /* four one-word sites per thread */
+      int qx, qy;
+      sweep_tile(g.L, g.tw, &qx, &qy, 4);
+      const int qyt = (g.L + qy - 1) / qy;
+      const dim3 qgrid(g.Lh / 4 / qx, qyt * g.ns, g.L / zc);
+      const cudaError_t e = g.occ == 4
+          ? launch_sweep(g, k_sweep<1, true, true, B1, false, 4>, qgrid, dim3(qx, qy), 0, st, g, p, ic,
+                         qyt, G, zc, g.pd, spin, d0, d1, jb, walk, rnd, t)
+          : launch_sweep(g, k_sweep<1, true, true, B0, false, 4>, qgrid, dim3(qx, qy), 0, st, g, p, ic,
+                         qyt, G, zc, g.pd, spin, d0, d1, jb, walk, rnd, t);
+      return e != cudaSuccess ? e : cudaGetLastError();
+    }
+  }
 #define MICSA_SWEEP(M, WD, B, T)                                                                  \
   do {                                                                                            \
     if (T && smem > 48 * 1024) {                                                                  \
@@ -1825,10 +1906,10 @@ cudaError_t micsa_launch_overlap(const micsa_geo &g, const uint32_t *spin, unsig
   return cudaGetLastError();
 }
 
-int micsa_sweep_wide_differs(int L) {
+int micsa_sweep_wide_differs(int L, int sites) {
   int a, b, c, d;
-  sweep_tile(L, 0, &a, &b);
-  sweep_tile(L, 1, &c, &d);
+  sweep_tile(L, 0, &a, &b, sites);
+  sweep_tile(L, 1, &c, &d, sites);
   return a != c;
 }
 

@@ -36,6 +36,7 @@ struct micsa_geo {
   int pdl;    /* 1: sweeps launched with programmatic dependent launch */
   int tw;     /* 1: sweep blocks span whole rows along x (when that differs) */
   int flow;   /* 1: an iteration's half-sweeps run as one dataflow launch */
+  int quad;   /* 1: four one-word sites per sweep thread (W = 1, direct loads) */
   int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */
@@ -63,8 +64,9 @@ cudaError_t micsa_make_tma(const micsa_geo &g, const uint32_t *d0, const uint32_
  * a TMA copy never completed; the sweep then read the words directly) */
 cudaError_t micsa_tma_timeout_count(unsigned *n);
 
-/* 1 if whole-row sweep blocks (micsa_geo.tw) differ from the default shape at this L */
-int micsa_sweep_wide_differs(int L);
+/* 1 if whole-row sweep blocks (micsa_geo.tw) differ from the default shape
+ * at this L, with 2 or 4 sites per thread */
+int micsa_sweep_wide_differs(int L, int sites = 2);
 
 /* slab depths the sweep can use for this L (divisors of L, ascending) */
 int micsa_sweep_zc_candidates(int L, int *out, int max);

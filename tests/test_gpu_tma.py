@@ -158,3 +158,43 @@ def test_whole_row_blocks_match_oracle(L, nr, nc, ns, split, pipe):
             g0, g1 = ctx.download_demons(s)
             assert np.array_equal(ge, e) and np.array_equal(go, o), s
             assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
+
+
+@pytest.mark.parametrize("L,nc,ns,split,occ,zc,pd,tile", [(32, 6, 2, 0, 4, 4, 2, None),
+                                                        (40, 3, 1, 0, 3, 8, 0, None),
+                                                        (96, 5, 2, 1, 4, 4, 2, "row"),
+                                                        (24, 2, 3, 0, 3, 2, 0, None),
+                                                        (64, 6, 2, 1, 3, 8, 4, "row")])
+def test_four_site_threads_match_oracle(L, nc, ns, split, occ, zc, pd, tile):
+    """32 replicas (one word per site) with four sites per thread (load=quad:
+    16-byte loads; demon words loaded one by one when the walk's x shift is
+    not a multiple of four x/2 steps), against the oracle over every walk
+    shift, with rows of 3 to 12 four-site groups."""
+    nr = 32
+    env = {"MICSA_SWEEP_ZC": str(zc), "MICSA_SWEEP_PD": str(pd), "MICSA_SWEEP_QUAD": "1",
+           "MICSA_SWEEP_SPLIT": str(split), "MICSA_SWEEP_OCC": str(occ), "MICSA_RESIDENT": "0"}
+    if tile:
+        env["MICSA_SWEEP_TILE"] = tile
+    old = _pinned(env)
+    try:
+        ctx = micsa.Context(L, nr, ns, nc)
+        assert "load=quad" in ctx.tuning(), ctx.tuning()
+    finally:
+        _restore(old)
+    rng = np.random.default_rng(19 * L + ns)
+    st = random_state(rng, L, nr, nc, ns)
+    iters = L // 2 + 3
+    with ctx:
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            ctx.upload_couplings(s, J)
+            ctx.upload_spins(s, e, o)
+            ctx.upload_demons(s, w0, w1)
+        ctx.iterate(iters)
+        ctx.synchronize()
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            for _ in range(iters):
+                oracle.micsa_iteration(L, nr, nc, J, e, o, w0, w1, 8)
+            ge, go = ctx.download_spins(s)
+            g0, g1 = ctx.download_demons(s)
+            assert np.array_equal(ge, e) and np.array_equal(go, o), s
+            assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
