@@ -157,7 +157,9 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
 
 /* Text line describing the launch shape the context's autotuner chose at
  * creation: "zc=<z planes per thread> pd=<L2 prefetch distance> split=<0: one
- * launch for all samples, 1: sample-major, one launch per sample>
+ * launch for all samples, k > 0: group-major, one launch per group of k
+ * samples (1: sample-major; the tuner times 0 and 1, MICSA_SWEEP_SPLIT=k
+ * pins larger groups)>
  * occ=<blocks per SM the registers are allocated for> load=<direct | tma:
  * demon tiles staged by TMA | async: operands double-buffered by cp.async |
  * pipe: each z step's loads issued one step ahead into registers |

@@ -45,7 +45,8 @@ struct micsa_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   int64_t launches = 0;
   int resident = 0;        /* small lattice: iterations run in shared memory */
-  int split = 0;           /* 1: one half-sweep launch per sample (smaller L2 working set) */
+  int split = 0;           /* k > 0: half-sweep launches per group of k samples, group-major
+                              (a smaller L2 working set); 0: all samples per launch */
   micsa_tma tma = {};      /* tensor maps of the demon arrays (staged sweep) */
   int64_t graph_launches = 0; /* kernels per replay of the iteration graph */
   int ntune = 0;           /* launch shapes timed at creation */
@@ -180,18 +181,18 @@ void parallel_for(int64_t n, int64_t grain, F f) {
   for (auto &th : pool) th.join();
 }
 
-/* One micSA half-sweep: of every sample in one launch (s < 0), or of sample
- * s alone -- the launch then sees only that sample's spins, couplings and
- * demon planes through offset pointers. */
-cudaError_t launch_half(micsa_ctx *ctx, const micsa_geo &g, int s, int p, int ic,
+/* One micSA half-sweep of samples s .. s+n-1 in one launch: of every sample
+ * (s = 0, n = ns), or of a group -- the launch then sees only the group's
+ * spins, couplings and demon planes through offset pointers. */
+cudaError_t launch_half(micsa_ctx *ctx, const micsa_geo &g, int s, int n, int p, int ic,
                         int64_t *launches) {
   if (launches) ++*launches;
-  if (s < 0)
+  if (s == 0 && n == g.ns)
     return micsa_launch_sweep_micsa(g, p, ic, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb, ctx->walk,
                                     &ctx->tma, ctx->stream);
   const size_t PW = (size_t)g.P * g.W;
   micsa_geo g1 = g;
-  g1.ns = 1;
+  g1.ns = n;
   g1.s0 = s; /* the staged sweep addresses the whole demon arrays */
   g1.active = g.active ? g.active + s : nullptr; /* a frozen sample returns at once */
   return micsa_launch_sweep_micsa(g1, p, ic, ctx->spin + s * 2 * PW,
@@ -202,28 +203,26 @@ cudaError_t launch_half(micsa_ctx *ctx, const micsa_geo &g, int s, int p, int ic
 }
 
 /* The half-sweeps of one iteration (ic = ic0 .. ic1-1).  split = 0: plane by
- * plane, all samples per launch.  split = 1: sample-major, all of sample 0's
- * half-sweeps, then sample 1's, ...: the spins that stay hot in L2 across
- * consecutive launches are one sample's.  g.flow (whole iterations): one
- * dataflow launch, its tiles in the same two orders. */
+ * plane, all samples per launch.  split = k > 0: group-major, all half-sweeps
+ * of samples 0 .. k-1 (one launch each), then of the next k, ...: the spins
+ * that stay hot in L2 across consecutive launches are one group's (k = 1:
+ * sample-major).  g.flow (whole iterations): one dataflow launch, its tiles
+ * sample-major (split > 0) or half-sweep-major. */
 cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0, int ic1,
                           int64_t *launches) {
   cudaError_t e = cudaSuccess;
   if (g.flow && ic0 == 0 && ic1 == g.nc) { /* the whole iteration in one dataflow launch */
     if (launches) ++*launches;
-    return micsa_launch_sweep_flow(g, split, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb, ctx->walk,
-                                   ctx->flow_ctl, ctx->stream);
+    return micsa_launch_sweep_flow(g, split > 0, ctx->spin, ctx->dem0, ctx->dem1, ctx->jb,
+                                   ctx->walk, ctx->flow_ctl, ctx->stream);
   }
-  if (!split) {
+  const int k = split > 0 && split < g.ns ? split : g.ns;
+  for (int s = 0; s < g.ns; s += k)
     for (int ic = ic0; ic < ic1; ic++)
       for (int p = 0; p < 2; p++)
-        if ((e = launch_half(ctx, g, -1, p, ic, launches)) != cudaSuccess) return e;
-    return e;
-  }
-  for (int s = 0; s < g.ns; s++)
-    for (int ic = ic0; ic < ic1; ic++)
-      for (int p = 0; p < 2; p++)
-        if ((e = launch_half(ctx, g, s, p, ic, launches)) != cudaSuccess) return e;
+        if ((e = launch_half(ctx, g, s, s + k <= g.ns ? k : g.ns - s, p, ic, launches)) !=
+            cudaSuccess)
+          return e;
   return e;
 }
 
@@ -275,7 +274,7 @@ int autotune(micsa_ctx *ctx) {
                *et = getenv("MICSA_SWEEP_TMA"), *ea = getenv("MICSA_SWEEP_ASYNC"),
                *ep2 = getenv("MICSA_SWEEP_PIPE"), *ew = getenv("MICSA_SWEEP_TILE"),
                *ef = getenv("MICSA_SWEEP_FLOW"), *eq = getenv("MICSA_SWEEP_QUAD");
-    ctx->split = es && atoi(es) && g.ns > 1;
+    ctx->split = es && atoi(es) > 0 && g.ns > 1 ? (atoi(es) < g.ns ? atoi(es) : g.ns) : 0;
     g.tma = et && atoi(et) && ctx->tma.ok;
     g.async = ea && atoi(ea) && g.W == 2 && !g.tma;
     g.pipe = ep2 && atoi(ep2) && !g.tma && !g.async;
@@ -334,6 +333,12 @@ int autotune(micsa_ctx *ctx) {
   const char *ef0 = getenv("MICSA_SWEEP_FLOW");
   const bool try_flow = !(ef0 && !strcmp(ef0, "0")) && g.L >= 128;
   const int reps = 3;
+  /* sample orders: all samples per launch, or sample-major.  Launches per
+   * group of 2 to 8 samples (MICSA_SWEEP_SPLIT=k) are not timed: alone they
+   * beat both at L=96 x 16 samples (7.28 against 6.76 attempts/ps), but the
+   * server's pools, tuned alone and run side by side, lost 9 to 12% of their
+   * throughput with them */
+  const int sps[2] = {0, 1}, nsp = g.ns > 1 ? 2 : 1;
   const int nocc = g.W % 4 ? 2 : 1; /* the 4-blocks variant exists for VW <= 2 */
   /* tm: 0 direct loads, 1 TMA-staged demon tiles, 2 cp.async double buffer (W = 2),
    * 3 loads pipelined one step ahead in registers (register budget for 3 or 2
@@ -343,7 +348,7 @@ int autotune(micsa_ctx *ctx) {
   for (int tm = 0; tm < 6; tm++)
   for (int tw = 0; tw < (tm == 5 ? ntw4 : ntw); tw++)
   for (int oc = 0; oc < nocc; oc++)
-  for (int sp = 0; sp < (g.ns > 1 ? 2 : 1); sp++)
+  for (int si = 0; si < nsp; si++)
   for (int c = 0; c < nz; c++)
     for (int d = 0; d < 3; d++) {
       if (pds[d] && pds[d] >= zcs[c]) continue; /* prefetch only within a slab */
@@ -351,6 +356,7 @@ int autotune(micsa_ctx *ctx) {
       if (tm == 2 && (g.W != 2 || pds[d])) continue;          /* no L2 prefetch there */
       if (tw && (tm == 1 || tm == 2)) continue; /* whole-row blocks: direct and pipelined loads */
       if ((tm == 4 && !try_flow) || (tm == 5 && g.W != 1)) continue;
+      const int sp = sps[si];
       g.zc = zcs[c];
       g.pd = pds[d];
       g.occ = tm == 3 ? (oc ? 2 : 3) : (oc ? 4 : 3);

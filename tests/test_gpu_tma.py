@@ -198,3 +198,40 @@ def test_four_site_threads_match_oracle(L, nc, ns, split, occ, zc, pd, tile):
             g0, g1 = ctx.download_demons(s)
             assert np.array_equal(ge, e) and np.array_equal(go, o), s
             assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
+
+
+@pytest.mark.parametrize("L,nr,nc,ns,split,quad", [(32, 64, 4, 5, 2, 0), (24, 32, 3, 3, 2, 1),
+                                                   (40, 64, 2, 4, 3, 0)])
+def test_sample_groups_match_oracle(L, nr, nc, ns, split, quad):
+    """Half-sweep launches per group of `split` samples (group-major; the last
+    group shorter), with a sample frozen for a while, against the oracle over
+    every walk shift."""
+    old = _pinned({"MICSA_SWEEP_ZC": "4", "MICSA_SWEEP_PD": "2", "MICSA_SWEEP_SPLIT": str(split),
+                   "MICSA_SWEEP_QUAD": str(quad), "MICSA_SWEEP_OCC": "4", "MICSA_RESIDENT": "0"})
+    try:
+        ctx = micsa.Context(L, nr, ns, nc)
+        assert "split=%d" % split in ctx.tuning(), ctx.tuning()
+    finally:
+        _restore(old)
+    rng = np.random.default_rng(23 * L + ns)
+    st = random_state(rng, L, nr, nc, ns)
+    frozen = ns - 2
+    a, b, c = 3, L // 2, 2
+    with ctx:
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            ctx.upload_couplings(s, J)
+            ctx.upload_spins(s, e, o)
+            ctx.upload_demons(s, w0, w1)
+        ctx.iterate(a)
+        ctx.set_active([0 if s == frozen else 1 for s in range(ns)])
+        ctx.iterate(b)
+        ctx.set_active(None)
+        ctx.iterate(c)
+        ctx.synchronize()
+        for s, (J, e, o, w0, w1, _) in enumerate(st):
+            for _ in range(a + c + (0 if s == frozen else b)):
+                oracle.micsa_iteration(L, nr, nc, J, e, o, w0, w1, 8)
+            ge, go = ctx.download_spins(s)
+            g0, g1 = ctx.download_demons(s)
+            assert np.array_equal(ge, e) and np.array_equal(go, o), s
+            assert np.array_equal(g0, w0) and np.array_equal(g1, w1), s
