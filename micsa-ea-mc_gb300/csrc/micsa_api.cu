@@ -52,7 +52,7 @@ struct micsa_ctx {
   int ntune = 0;           /* launch shapes timed at creation */
   int tune_zc[MICSA_TUNE_MAX] = {0}, tune_pd[MICSA_TUNE_MAX] = {0};
   int tune_split[MICSA_TUNE_MAX] = {0}, tune_occ[MICSA_TUNE_MAX] = {0};
-  int tune_tma[MICSA_TUNE_MAX] = {0}, tune_tw[MICSA_TUNE_MAX] = {0};
+  int tune_load[MICSA_TUNE_MAX] = {0}, tune_tw[MICSA_TUNE_MAX] = {0}; /* load: 0 direct .. 5 quad */
   double tune_ms[MICSA_TUNE_MAX] = {0};
   int tune_cached = 0; /* the shape came from an earlier context's timing */
   /* demon refresh on the device: jump tables of one segment length */
@@ -232,7 +232,7 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
  * many contexts of a few shapes pay for each shape once. */
 struct tune_entry {
   int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, n;
-  std::vector<int> zcs, pds, splits, occs, tmas, tws;
+  std::vector<int> zcs, pds, splits, occs, loads, tws;
   std::vector<double> ms;
 };
 std::mutex tune_mu;
@@ -309,7 +309,7 @@ int autotune(micsa_ctx *ctx) {
         ctx->tune_pd[c] = t.pds[c];
         ctx->tune_split[c] = t.splits[c];
         ctx->tune_occ[c] = t.occs[c];
-        ctx->tune_tma[c] = t.tmas[c];
+        ctx->tune_load[c] = t.loads[c];
         ctx->tune_tw[c] = t.tws[c];
         ctx->tune_ms[c] = t.ms[c];
       }
@@ -397,7 +397,7 @@ int autotune(micsa_ctx *ctx) {
         ctx->tune_pd[n] = g.pd;
         ctx->tune_split[n] = sp;
         ctx->tune_occ[n] = g.occ;
-        ctx->tune_tma[n] = tm;
+        ctx->tune_load[n] = tm;
         ctx->tune_tw[n] = tw;
         ctx->tune_ms[n] = per;
         n++;
@@ -446,7 +446,7 @@ int autotune(micsa_ctx *ctx) {
     t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
     t.splits.assign(ctx->tune_split, ctx->tune_split + n);
     t.occs.assign(ctx->tune_occ, ctx->tune_occ + n);
-    t.tmas.assign(ctx->tune_tma, ctx->tune_tma + n);
+    t.loads.assign(ctx->tune_load, ctx->tune_load + n);
     t.tws.assign(ctx->tune_tw, ctx->tune_tw + n);
     t.ms.assign(ctx->tune_ms, ctx->tune_ms + n);
     std::lock_guard<std::mutex> lk(tune_mu);
@@ -592,7 +592,7 @@ int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
                    ctx->g.tw ? "row" : "default", ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
     k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],
-                  ctx->tune_pd[c], ctx->tune_split[c], ctx->tune_occ[c], ctx->tune_tma[c],
+                  ctx->tune_pd[c], ctx->tune_split[c], ctx->tune_occ[c], ctx->tune_load[c],
                   ctx->tune_tw[c], ctx->tune_ms[c]);
   return MICSA_OK;
 }
