@@ -54,3 +54,18 @@ def test_reference_arm_prints_one_line_from_rank_zero():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_roofline_traffic_comes_from_the_profile_of_the_tuned_kernel():
+    """bench.py's roofline.traffic is read from the committed ncu summary of
+    the kernel the autotuner picked (the dataflow sweep or the per-launch
+    sweep), and scaled by sites only from a capture of that same kernel."""
+    sys.path.insert(0, ROOT)
+    import bench
+    dep, note = bench.traffic_per_launch(160, 64, 2, "k_sweep_dep")
+    plain, note2 = bench.traffic_per_launch(160, 64, 2, "k_sweep")
+    assert dep and plain and dep != plain
+    assert "k_sweep_dep" in note and "this shape" in note and "this shape" in note2
+    scaled, note3 = bench.traffic_per_launch(80, 64, 2, "k_sweep")
+    assert scaled == plain / 8 and "scaled by sites" in note3
+    assert bench.traffic_per_launch(160, 64, 2, "no_such_kernel") == (None, None)
