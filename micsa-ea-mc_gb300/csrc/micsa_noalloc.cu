@@ -20,6 +20,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
+
 #include "micsa.h"
 
 /* Per-replica counters of unsatisfied bonds, shared by every call on a
@@ -92,23 +94,27 @@ __global__ void k_energy_ref_finish(int n, long long threeV,
   if (i < n) e_spin[i] = (int32_t)(threeV - 2LL * (long long)counters[i]);
 }
 
-/* device address of the counters, looked up once per device */
+/* device address of the counters, looked up once per device (threads that
+ * make their first call on a device at the same time look it up alike and
+ * store the same address) */
 unsigned long long *counters_on(int device, char *err, size_t errlen) {
-  static unsigned long long *addr[64] = {nullptr};
+  static std::atomic<unsigned long long *> addr[64];
   if (device < 0 || device >= 64) {
     if (err) snprintf(err, errlen, "device %d out of range", device);
     return nullptr;
   }
-  if (!addr[device]) {
+  unsigned long long *a = addr[device].load(std::memory_order_acquire);
+  if (!a) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, micsa_noalloc_counters);
     if (e != cudaSuccess) {
       if (err) snprintf(err, errlen, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
       return nullptr;
     }
-    addr[device] = (unsigned long long *)p;
+    a = (unsigned long long *)p;
+    addr[device].store(a, std::memory_order_release);
   }
-  return addr[device];
+  return a;
 }
 
 }  // namespace
