@@ -196,3 +196,20 @@ def test_seed_fanout_paranoia_constant():
     a = micsa.seeds_from_one(12345, 8)[1]
     b = micsa.seeds_from_one(12345, 8)[1]
     assert np.array_equal(a, b) and len(set(a.tolist())) == 8
+
+
+def test_every_environment_variable_is_documented():
+    """Every MICSA_* variable the library or the driver reads appears in the
+    integration notes' table."""
+    import glob
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    names = set()
+    for f in (glob.glob(os.path.join(root, "micsa-ea-mc_gb300", "csrc", "*.cu")) +
+              glob.glob(os.path.join(root, "micsa-ea-mc_gb300", "host", "*.c"))):
+        names |= set(re.findall(r'getenv\("(MICSA_[A-Z_]+)"\)', open(f).read()))
+    doc = open(os.path.join(root, "INTEGRATION.md")).read()
+    short = set(re.findall(r"`_([A-Z]+)`", doc))  # the MICSA_SWEEP_* list written as `_PD`, ...
+    missing = [n for n in sorted(names)
+               if n not in doc and not (n.startswith("MICSA_SWEEP_") and n[12:] in short)]
+    assert names and not missing, missing
