@@ -387,14 +387,16 @@ def e2e_upload_every_step(a, dist, ctx, demons, attempts):
 
 
 def cpu_state(L, nr, ns, nc, seed=7):
-    """Seeded random reference-layout state for the CPU arms (same shapes)."""
-    import micsa
+    """Seeded random reference-layout state for the CPU arms (same shapes).
+    Everything here comes from numpy and the oracle's own packer (packing_J,
+    ini.c:521-578): the CPU arms never load the product library."""
+    import oracle
     rng = np.random.default_rng(seed)
     H = (L // 4) ** 3 // 2
     out = []
     for _ in range(ns):
-        J = micsa.pack_couplings(L, *(rng.integers(0, 2, size=L ** 3, dtype=np.uint8)
-                                      for _ in range(3)))
+        J = oracle.pack_couplings(L, *(rng.integers(0, 2, size=L ** 3, dtype=np.uint8)
+                                       for _ in range(3)))
         e = rng.integers(0, 2 ** 63, size=H * nr, dtype=np.uint64)
         o = rng.integers(0, 2 ** 63, size=H * nr, dtype=np.uint64)
         w0 = rng.integers(0, 2 ** 63, size=2 * H * nc * nr, dtype=np.uint64)
@@ -441,9 +443,13 @@ def run_reference(a):
 
 
 def config(a):
-    return {"workload": "plain micSA, L=%d periodic +-J lattice, %d samples x %d replicas "
-                        "(uint32 words), nc=%d demons/site; step = one iteration = %d half-sweeps "
-                        "+ demon walk" % (a.L, a.nsamples, a.nr, a.nc, 2 * a.nc),
+    return {"workload": "plain micSA, L=%d periodic +-J lattice, %d samples x %d replicas, "
+                        "nc=%d demons/site; step = one iteration = %d half-sweeps + demon walk"
+                        % (a.L, a.nsamples, a.nr, a.nc, 2 * a.nc),
+            "words": "the %d replicas of a site sit in %d uint32 words moved as one %d-byte "
+                     "vector: bit-identical to the reference's uint64 multispin words, the "
+                     "bitwise arithmetic done on 32-bit lanes (dtype u32)"
+                     % (a.nr, a.nr // 32, a.nr // 8),
             "L": a.L, "replicas": a.nr, "samples": a.nsamples, "nc": a.nc,
             "beta": BETA, "l2": "inputs larger than L2: each step streams %.0f MB of demon planes"
                                 % (a.nsamples * 2 * a.nc * 2 * a.L ** 3 / 2 * a.nr / 8 / 1e6),

@@ -20,6 +20,20 @@
  * Calls on one context must come from one thread at a time.  All device work
  * is issued on the context's own stream; calls that return data to the host
  * synchronise that stream.
+ *
+ * Environment variables the library reads (all optional):
+ *   MICSA_SWEEP_ZC, MICSA_SWEEP_PD, MICSA_SWEEP_SPLIT, MICSA_SWEEP_OCC,
+ *   MICSA_SWEEP_TILE, MICSA_SWEEP_TMA, MICSA_SWEEP_ASYNC, MICSA_SWEEP_PIPE,
+ *   MICSA_SWEEP_FLOW, MICSA_SWEEP_QUAD   pin the sweep's launch shape at
+ *                        micsa_create (meanings at micsa_tuning_report)
+ *   MICSA_TUNE_CACHE=0   time every context instead of reusing the process's
+ *                        choice for its shape
+ *   MICSA_RESIDENT=0     keep L <= 16 on the per-half-sweep kernels
+ *   MICSA_PDL=0          plain launches instead of programmatic dependent launch
+ *   MICSA_REFRESH_WPS=n  segment length of the GPU demon refresh, in words
+ *   MICSA_REFRESH_OCC=1  the refresh kernel without its register budget
+ * The command-line driver micsa_run adds MICSA_REFRESH=host,
+ * MICSA_HOST_THREADS=n and MICSA_OBSERVABLES=1 (see its usage comment).
  */
 #ifndef MICSA_H
 #define MICSA_H
@@ -44,7 +58,7 @@ typedef struct micsa_ctx micsa_ctx;
 
 typedef struct {
   int device;   /* CUDA device ordinal (argv[7], main.cu:39,52-59) */
-  int L;        /* lattice side: multiple of 8, 8..1024 (header.h:38-40) */
+  int L;        /* lattice side: multiple of 8, 8..888 (header.h:38-40; int32 energies) */
   int nr;       /* replicas per sample, multiple of 32 (header.h:17 NR) */
   int nsamples; /* samples simulated together, 1..4096 (nbits, main.cu:64) */
   int nc;       /* demons per site, 1..6 (input.in line 6; d_Walk limit main.cu:1082) */
@@ -186,23 +200,30 @@ int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n);
  * call cudaMalloc when they measure: processes that size their device memory
  * once at start-up (services, real-time loops), whose device memory belongs
  * to another allocator, or that must not let an allocation synchronise their
- * streams.  The caller passes device pointers to the reference's own
- * device-resident words of nsamples samples, concatenated by sample:
- *   even, odd  [s][H][nr] uint64   (d_spin, CopyDataOnDevice main.cu:429-434)
- *   J          [s][12][H] uint64   (d_J,    CopyDataOnDevice main.cu:436-455)
- * and a device int32 output e_spin[s*nr + r] (h_Ener of Measure_Energy_Spins).
- * Work is queued on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * streams.  The caller passes the reference's own device rows through the
+ * host-side pointer tables the reference keeps for them (mmcuda,
+ * main.cu:1219-1289, filled by CopyDataOnDevice, main.cu:404-471), one
+ * table entry per row, samples one after another:
+ *   spin_rows[2*s + p]   = h_spin[s][p], p = 0 even, 1 odd: [H][nr] uint64
+ *   J_rows[12*s + k]     = h_J[s][k], k = colour*6 + direction: [H] uint64
+ * (host arrays of device pointers, read during the call only) and a device
+ * int32 output e_spin[s*nr + r] (h_Ener of Measure_Energy_Spins,
+ * main.cu:315-336).  Work is queued on `stream` (a cudaStream_t; NULL = the
+ * legacy default stream).  L must be a multiple of 8 in [8, 888]: the
+ * energies are int32, as the reference's h_Ener, and |E| <= 3 L^3.
  * The per-replica counters live in one fixed device array of
  * MICSA_NOALLOC_MAX_REPLICAS entries per GPU, kept until the process exits:
  * nr * nsamples above that limit is rejected with MICSA_ERR_ARG.  Every call
  * shares the array (each call zeroes the part it uses), so calls that overlap
- * on the GPU race: keep them in one stream or otherwise ordered.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress
- * on the current device); make that first call before any stream capture.
- * err (optional) receives a message on failure. */
+ * on the GPU race: keep them in one stream or otherwise ordered.  Each call
+ * looks up the array's address in the current device's context; the first
+ * call on a device also loads the library's device code there, so make that
+ * first call before any stream capture.  err (optional) receives a message
+ * on failure. */
 #define MICSA_NOALLOC_MAX_REPLICAS 8192
-int micsa_energy_noalloc(int L, int nr, int nsamples, const uint64_t *even, const uint64_t *odd,
-                         const uint64_t *J, int32_t *e_spin, void *stream, char *err,
+#define MICSA_NOALLOC_MAX_L 888
+int micsa_energy_noalloc(int L, int nr, int nsamples, const uint64_t *const *spin_rows,
+                         const uint64_t *const *J_rows, int32_t *e_spin, void *stream, char *err,
                          size_t errlen);
 
 /* ---- Batched runs: no counterpart in the reference ----

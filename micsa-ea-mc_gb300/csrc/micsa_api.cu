@@ -115,8 +115,10 @@ sizes sizes_of(const micsa_config &c) {
 
 int check_cfg(const micsa_config *c, char *msg, size_t n) {
   if (!c) return snprintf(msg, n, "null configuration"), MICSA_ERR_ARG;
-  if (c->L < 8 || c->L > 1024 || c->L % 8)
-    return snprintf(msg, n, "L=%d must be a multiple of 8 in [8, 1024]", c->L), MICSA_ERR_ARG;
+  /* int32 energies (the reference's int h_Ener): |E| <= 3 L^3 < 2^31 up to L = 888 */
+  if (c->L < 8 || c->L > 888 || c->L % 8)
+    return snprintf(msg, n, "L=%d must be a multiple of 8 in [8, 888] (int32 energies)", c->L),
+           MICSA_ERR_ARG;
   if (c->nr < 32 || c->nr % 32)
     return snprintf(msg, n, "nr=%d must be a positive multiple of 32", c->nr),
            MICSA_ERR_UNSUPPORTED;

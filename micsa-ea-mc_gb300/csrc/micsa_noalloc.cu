@@ -12,15 +12,17 @@
  * file-scope device array instead.  The caller owns and passes every input
  * and output buffer; nothing here allocates or frees device memory.
  *
- * The inputs are the reference's own device-resident layouts (the words
- * CopyDataOnDevice keeps in d_spin and d_J, PROGRAM/src/main.cu:429-455),
- * so a caller that already holds them needs no conversion.
+ * The inputs are the reference's own device rows, passed as the host-side
+ * tables of device pointers the reference keeps: h_spin[s][p] (two rows per
+ * sample, [H][nr] words each) and h_J[s][k] (twelve rows per sample, [H]
+ * words each), both filled by mmcuda and CopyDataOnDevice
+ * (PROGRAM/src/main.cu:404-471,1219-1289).  The row pointers travel to the
+ * kernel by value, a chunk of samples per launch, so no table is copied to
+ * the device.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
-
-#include <atomic>
 
 #include "micsa.h"
 
@@ -29,6 +31,13 @@
 static __device__ __align__(256) unsigned long long micsa_noalloc_counters[MICSA_NOALLOC_MAX_REPLICAS];
 
 namespace {
+
+constexpr int ROWS_PER_LAUNCH = 16; /* samples whose row pointers one launch carries */
+
+struct sample_rows {
+  const uint64_t *spin[ROWS_PER_LAUNCH][2];
+  const uint64_t *J[ROWS_PER_LAUNCH][12];
+};
 
 /* block-edge rotations of the reference words (main.cu:706-742) */
 __device__ __forceinline__ uint64_t rot_dir(int d, uint64_t v) {
@@ -44,16 +53,16 @@ __device__ __forceinline__ uint64_t rot_dir(int d, uint64_t v) {
 
 /* Unsatisfied bonds of the colour-0 words, per replica (the counting of
  * d_computeEne, main.cu:745-815, on the reference layout).  Thread = replica
- * r and a stride of words h; blockIdx.y = sample.  Each word holds 64 sites
- * of one replica, so a popcount is already a per-replica count. */
-__global__ void k_energy_ref(int L, int nr, const uint64_t *__restrict__ even,
-                             const uint64_t *__restrict__ odd, const uint64_t *__restrict__ J,
+ * r and a stride of words h; blockIdx.y = sample within this launch's chunk.
+ * Each word holds 64 sites of one replica, so a popcount is already a
+ * per-replica count. */
+__global__ void k_energy_ref(int L, int nr, const sample_rows rows,
                              unsigned long long *__restrict__ counters) {
   const int s = blockIdx.y;
   const int m = L / 4, mh = m / 2;
   const int64_t H = (int64_t)m * m * m / 2;
-  const uint64_t *ev = even + (int64_t)s * H * nr, *od = odd + (int64_t)s * H * nr;
-  const uint64_t *Js = J + (int64_t)s * 12 * H;
+  const uint64_t *__restrict__ ev = rows.spin[s][0];
+  const uint64_t *__restrict__ od = rows.spin[s][1];
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int r = (int)(t % nr);
   const int64_t chunks = ((int64_t)gridDim.x * blockDim.x) / nr;
@@ -71,7 +80,7 @@ __global__ void k_energy_ref(int L, int nr, const uint64_t *__restrict__ even,
     for (int d = 0; d < 6; d++) {
       const int64_t nh = (na[d] + (int64_t)m * nb[d] + (int64_t)m * m * nc[d]) / 2;
       uint64_t n = od[nh * nr + r];
-      const uint64_t jw = Js[(int64_t)d * H + h];
+      const uint64_t jw = rows.J[s][d][h]; /* colour-0 rows are k = d */
       uint64_t f;
       if (d < 3) {
         if (wrap[d]) n = rot_dir(d, n);
@@ -94,37 +103,22 @@ __global__ void k_energy_ref_finish(int n, long long threeV,
   if (i < n) e_spin[i] = (int32_t)(threeV - 2LL * (long long)counters[i]);
 }
 
-/* device address of the counters, looked up once per device (threads that
- * make their first call on a device at the same time look it up alike and
- * store the same address) */
-unsigned long long *counters_on(int device, char *err, size_t errlen) {
-  static std::atomic<unsigned long long *> addr[64];
-  if (device < 0 || device >= 64) {
-    if (err) snprintf(err, errlen, "device %d out of range", device);
-    return nullptr;
-  }
-  unsigned long long *a = addr[device].load(std::memory_order_acquire);
-  if (!a) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, micsa_noalloc_counters);
-    if (e != cudaSuccess) {
-      if (err) snprintf(err, errlen, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-      return nullptr;
-    }
-    a = (unsigned long long *)p;
-    addr[device].store(a, std::memory_order_release);
-  }
-  return a;
-}
-
 }  // namespace
 
-extern "C" int micsa_energy_noalloc(int L, int nr, int nsamples, const uint64_t *even,
-                                    const uint64_t *odd, const uint64_t *J, int32_t *e_spin,
+extern "C" int micsa_energy_noalloc(int L, int nr, int nsamples,
+                                    const uint64_t *const *spin_rows,
+                                    const uint64_t *const *J_rows, int32_t *e_spin,
                                     void *stream, char *err, size_t errlen) {
   if (err && errlen) err[0] = 0;
-  if (L < 8 || L > 1024 || L % 8 || nr < 1 || nsamples < 1 || !even || !odd || !J || !e_spin) {
-    if (err) snprintf(err, errlen, "invalid arguments (L=%d nr=%d nsamples=%d)", L, nr, nsamples);
+  /* 3*L^3 must fit the int32 energies (the reference's int h_Ener has the
+   * same bound): L <= 888 */
+  if (L < 8 || L > MICSA_NOALLOC_MAX_L || L % 8 || nr < 1 || nsamples < 1 || !spin_rows ||
+      !J_rows || !e_spin) {
+    if (err)
+      snprintf(err, errlen,
+               "invalid arguments (L=%d must be a multiple of 8 in [8, %d]; nr=%d, nsamples=%d "
+               "must be positive; row tables and output must be given)",
+               L, MICSA_NOALLOC_MAX_L, nr, nsamples);
     return MICSA_ERR_ARG;
   }
   if ((long long)nr * nsamples > MICSA_NOALLOC_MAX_REPLICAS) {
@@ -133,24 +127,43 @@ extern "C" int micsa_energy_noalloc(int L, int nr, int nsamples, const uint64_t 
                (long long)nr * nsamples, MICSA_NOALLOC_MAX_REPLICAS);
     return MICSA_ERR_ARG;
   }
-  int device = 0;
-  cudaError_t e = cudaGetDevice(&device);
+  for (int i = 0; i < 2 * nsamples; i++)
+    if (!spin_rows[i]) {
+      if (err) snprintf(err, errlen, "spin row %d (sample %d) is NULL", i, i / 2);
+      return MICSA_ERR_ARG;
+    }
+  for (int i = 0; i < 12 * nsamples; i++)
+    if (!J_rows[i]) {
+      if (err) snprintf(err, errlen, "coupling row %d (sample %d) is NULL", i, i / 12);
+      return MICSA_ERR_ARG;
+    }
+  /* The array's device address in the current device's context, looked up
+   * on every call: a lookup allocates nothing, and a cached address would
+   * go stale if the caller reset the device and a new context reloaded this
+   * module.  The first call on a device also loads the module there. */
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, micsa_noalloc_counters);
   if (e != cudaSuccess) {
-    if (err) snprintf(err, errlen, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (err) snprintf(err, errlen, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
     return MICSA_ERR_CUDA;
   }
-  unsigned long long *counters = counters_on(device, err, errlen);
-  if (!counters) return MICSA_ERR_CUDA;
+  unsigned long long *counters = (unsigned long long *)p;
   cudaStream_t st = (cudaStream_t)stream;
   const int n = nr * nsamples;
   e = cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (size_t)n, st);
-  if (e == cudaSuccess) {
-    const int64_t m = L / 4, H = m * m * m / 2;
-    int64_t chunks = H < 256 ? H : 256; /* words per replica handled in parallel */
-    int64_t threads = chunks * nr;
-    const int tpb = 256;
-    int blocks = (int)((threads + tpb - 1) / tpb);
-    k_energy_ref<<<dim3(blocks, nsamples), tpb, 0, st>>>(L, nr, even, odd, J, counters);
+  const int64_t m = L / 4, H = m * m * m / 2;
+  const int64_t chunks = H < 256 ? H : 256; /* words per replica handled in parallel */
+  const int tpb = 256;
+  const int blocks = (int)((chunks * nr + tpb - 1) / tpb);
+  for (int s0 = 0; e == cudaSuccess && s0 < nsamples; s0 += ROWS_PER_LAUNCH) {
+    const int cnt = nsamples - s0 < ROWS_PER_LAUNCH ? nsamples - s0 : ROWS_PER_LAUNCH;
+    sample_rows rows = {};
+    for (int s = 0; s < cnt; s++) {
+      rows.spin[s][0] = spin_rows[2 * (s0 + s)];
+      rows.spin[s][1] = spin_rows[2 * (s0 + s) + 1];
+      for (int k = 0; k < 12; k++) rows.J[s][k] = J_rows[12 * (s0 + s) + k];
+    }
+    k_energy_ref<<<dim3(blocks, cnt), tpb, 0, st>>>(L, nr, rows, counters + (int64_t)s0 * nr);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {

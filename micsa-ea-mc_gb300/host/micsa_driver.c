@@ -15,8 +15,12 @@
  * directory is "{dir}I%03d/" as io.c:661 intends (the reference formats it
  * with overlapping sprintf buffers); changentimes.in is parsed as "count
  * then times" (io.c:930-968 reads through an uninitialised pointer).
- * Setting MICSA_OBSERVABLES=1 also writes evol_q.txt, evol_C4.txt and evol_xi.txt
- * (correlation lengths xi12, xi23 from C4).
+ * Environment: MICSA_OBSERVABLES=1 also writes evol_q.txt, evol_C4.txt and
+ * evol_xi.txt (correlation lengths xi12, xi23 from C4); MICSA_REFRESH=host
+ * draws the demon refreshes on host threads (the reference's InitWalkers)
+ * instead of the GPU; MICSA_HOST_THREADS=n sets the host threads used for
+ * initialisation and host refreshes (default: all cores).  The library's own
+ * variables are listed in micsa.h.
  */
 #define _GNU_SOURCE
 #include <errno.h>

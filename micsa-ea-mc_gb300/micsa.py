@@ -29,6 +29,7 @@ ABI_SYMBOLS = [
     "micsa_server_create", "micsa_submit", "micsa_poll", "micsa_server_destroy",
 ]
 NOALLOC_MAX_REPLICAS = 8192
+NOALLOC_MAX_L = 888
 
 _lib = None
 

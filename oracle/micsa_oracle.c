@@ -474,3 +474,32 @@ int32_t oracle_scalar_energy(int L, const uint8_t *u, const uint8_t *Jx,
   int64_t V = (int64_t)L * L * L;
   return (int32_t)(3 * V - 2 * e);
 }
+
+/* packing_J (ini.c:521-578): coupling of site (x,y,z) along +d goes to bit
+ * bx + 4*by + 16*bz of the site's own forward word d and of its
+ * +d neighbour's backward word d+3 (ini.c:553-564); rows are then taken per
+ * colour in word order (viciniB/N, ini.c:569-575), which here is msc/2. */
+void oracle_pack_couplings(int L, const uint8_t *Jx, const uint8_t *Jy,
+                           const uint8_t *Jz, uint64_t *J) {
+  const int m = L / 4;
+  const int64_t H = half_words(L);
+  const uint8_t *Jd[3] = {Jx, Jy, Jz};
+  memset(J, 0, sizeof(uint64_t) * 12 * H);
+  for (int z = 0; z < L; z++)
+    for (int y = 0; y < L; y++)
+      for (int x = 0; x < L; x++) {
+        const int64_t site = x + (int64_t)L * y + (int64_t)L * L * z;
+        const int a = x % m, b = y % m, c = z % m;
+        const uint64_t bit = (uint64_t)(x / m + 4 * (y / m) + 16 * (z / m));
+        const int p = (a + b + c) & 1;
+        for (int d = 0; d < 3; d++) {
+          const int na = d == 0 ? (a + 1) % m : a, nb = d == 1 ? (b + 1) % m : b,
+                    nc = d == 2 ? (c + 1) % m : c;
+          const int64_t own = (a + (int64_t)m * b + (int64_t)m * m * c) / 2;
+          const int64_t nbr = (na + (int64_t)m * nb + (int64_t)m * m * nc) / 2;
+          const uint64_t v = (uint64_t)(Jd[d][site] & 1) << bit;
+          J[(int64_t)(p * 6 + d) * H + own] |= v;
+          J[(int64_t)((p ^ 1) * 6 + d + 3) * H + nbr] |= v;
+        }
+      }
+}

@@ -71,6 +71,11 @@ void oracle_demon_energy(int L, int nr, int nc, const uint64_t *w0,
 uint64_t oracle_isi_word(uint64_t j1, uint64_t j2, uint64_t j3, uint64_t j4,
                          uint64_t *D0, uint64_t *D1);
 
+/* coupling words J[(p*6 + d)*H + h] from per-site couplings J{x,y,z}[x +
+ * L*y + L*L*z] in {0,1} (packing_J, ini.c:521-578) */
+void oracle_pack_couplings(int L, const uint8_t *Jx, const uint8_t *Jy,
+                           const uint8_t *Jz, uint64_t *J);
+
 /* ---- plain scalar rendering on unpacked spins uu[r*V + x+L*y+L*L*z] ---- */
 /* accept/demon rule per site: returns new demon, sets *flip */
 int oracle_scalar_rule(int unsatisfied, int demon, int *flip);

@@ -15,7 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE = os.environ.get("MICSA_REFERENCE_DIR", "/root/reference")
+# the reference sources, where a copy exists (never on the GPU host); unset:
+# the live reference build is skipped and the committed golden fixtures pin
+# the oracle alone
+REFERENCE = os.environ.get("MICSA_REFERENCE_DIR", "")
 
 _lib = None
 
@@ -33,7 +36,7 @@ def build(force=False):
 
 
 def reference_available():
-    return os.path.exists(os.path.join(REFERENCE, "PROGRAM", "src", "main.cu"))
+    return bool(REFERENCE) and os.path.exists(os.path.join(REFERENCE, "PROGRAM", "src", "main.cu"))
 
 
 def build_reference(L, nr, ms=2):
@@ -74,6 +77,7 @@ def lib():
                                              u64p, u64p]),
             "oracle_overlap_c4": (None, [C.c_int, C.c_int, u8p, i64p, i64p]),
             "oracle_scalar_energy": (C.c_int32, [C.c_int, u8p, u8p, u8p, u8p]),
+            "oracle_pack_couplings": (None, [C.c_int, u8p, u8p, u8p, u64p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -158,6 +162,14 @@ def isi_word(j1, j2, j3, j4, d0, d1):
 def scalar_energy(L, u, Jx, Jy, Jz):
     return lib().oracle_scalar_energy(L, _p(np.ascontiguousarray(u, np.uint8), U8), _p(Jx, U8),
                                       _p(Jy, U8), _p(Jz, U8))
+
+
+def pack_couplings(L, Jx, Jy, Jz):
+    H = (L // 4) ** 3 // 2
+    J = np.zeros(12 * H, np.uint64)
+    src = [np.ascontiguousarray(a, np.uint8) for a in (Jx, Jy, Jz)]  # alive across the call
+    lib().oracle_pack_couplings(L, *(_p(a, U8) for a in src), _p(J, U64))
+    return J
 
 
 def tables(L):

@@ -5,7 +5,7 @@
 # for the HOST CPU, so that its own kernels and host code produce golden
 # outputs in a container without a GPU.
 #
-#   usage: build_ref.sh L NR [MAXNSAMPLES] [OUTDIR]
+#   usage: MICSA_REFERENCE_DIR=<reference checkout> build_ref.sh L NR [MAXNSAMPLES] [OUTDIR]
 #
 # Compile-time settings follow PROGRAM/Makefile:1-6 (-DNBETAS=1
 # -DNUMBITSPREBUSQUEDAS=10 -DJANUS -DWALK) with L from the command line.
@@ -21,7 +21,8 @@ NR=$2
 MS=${3:-2}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=${4:-$HERE/../_ref}
-REF=${MICSA_REFERENCE_DIR:-/root/reference}/PROGRAM
+[ -n "${MICSA_REFERENCE_DIR:-}" ] || { echo "MICSA_REFERENCE_DIR (the reference sources) is not set" >&2; exit 3; }
+REF=$MICSA_REFERENCE_DIR/PROGRAM
 [ -f "$REF/src/main.cu" ] || { echo "reference sources not found at $REF" >&2; exit 3; }
 mkdir -p "$OUT"
 OUT=$(cd "$OUT" && pwd)

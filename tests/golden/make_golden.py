@@ -6,10 +6,10 @@ stores what it wrote: the three evol_*.txt files verbatim, seeds.in and
 master_seedJ.in verbatim, and SHA-256 digests of conf_Js, of every conf.<t>
 record (spins, energies, generator states) and of the final walkers file.
 
-Needs the reference sources (default /root/reference, or
-MICSA_REFERENCE_DIR); run from the repository root:
+Needs the reference sources, named by MICSA_REFERENCE_DIR; run from the
+repository root:
 
-    python tests/golden/make_golden.py [case ...]
+    MICSA_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py [case ...]
 """
 import json
 import os

@@ -69,3 +69,28 @@ def test_roofline_traffic_comes_from_the_profile_of_the_tuned_kernel():
     scaled, note3 = bench.traffic_per_launch(80, 64, 2, "k_sweep")
     assert scaled == plain / 8 and "scaled by sites" in note3
     assert bench.traffic_per_launch(160, 64, 2, "no_such_kernel") == (None, None)
+
+
+def test_reference_arm_never_maps_the_product_library(tmp_path):
+    """The reference arm times the CPU restatement only: after a whole
+    `bench.py --impl reference` run in one process, libmicsa must not be among
+    the process's mappings (its ratio against the GPU arm would otherwise
+    compare the product with itself)."""
+    w = tmp_path / "ref_arm.py"
+    w.write_text(
+        "import sys\n"
+        "sys.path.insert(0, %r)\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--L', '8', '--nr', '32', '--nsamples',"
+        " '1', '--nc', '2', '--steps', '2', '--warmup', '1']\n"
+        "import bench\n"
+        "bench.main()\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('LIBMICSA_MAPPED', 'libmicsa' in maps, 'LIBORACLE_MAPPED', 'liboracle' in maps)\n"
+        % ROOT)
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    p = subprocess.run([sys.executable, str(w)], cwd=ROOT, stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=300, env=env)
+    assert p.returncode == 0, p.stdout[-3000:]
+    assert "LIBMICSA_MAPPED False LIBORACLE_MAPPED True" in p.stdout, p.stdout[-3000:]
+    line = json.loads(next(l for l in p.stdout.splitlines() if l.startswith("{")))
+    assert line["impl"] == "reference" and line["value"] > 0

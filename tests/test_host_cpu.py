@@ -118,6 +118,16 @@ def test_energy_equals_scalar_energy(L):
         assert en[r] == oracle.scalar_energy(L, uu[r * V:(r + 1) * V], Jx, Jy, Jz)
 
 
+@pytest.mark.parametrize("L", [8, 16, 24, 40])
+def test_oracle_coupling_packer_equals_product_packer(L):
+    """The oracle's packing_J restatement (used by the CPU arms of bench.py,
+    which must not load the product library) and the product's host packer
+    give the same coupling words."""
+    rng = np.random.default_rng(L + 17)
+    Jx, Jy, Jz = (rng.integers(0, 2, size=L ** 3, dtype=np.uint8) for _ in range(3))
+    assert np.array_equal(oracle.pack_couplings(L, Jx, Jy, Jz), micsa.pack_couplings(L, Jx, Jy, Jz))
+
+
 def test_walk_is_a_translation():
     """After k walks (d_Walk), the colour-p demon of plane ic sits at
     x + sgn*2k*e_axis of where it started (sgn = +1 iff (p == 0) == (ic < 3)):
@@ -199,17 +209,21 @@ def test_seed_fanout_paranoia_constant():
 
 
 def test_every_environment_variable_is_documented():
-    """Every MICSA_* variable the library or the driver reads appears in the
-    integration notes' table."""
+    """Every MICSA_* variable the library reads is listed in the public
+    header, and every one the command-line driver reads in the driver's
+    usage comment."""
     import glob
     import re
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    names = set()
-    for f in (glob.glob(os.path.join(root, "micsa-ea-mc_gb300", "csrc", "*.cu")) +
-              glob.glob(os.path.join(root, "micsa-ea-mc_gb300", "host", "*.c"))):
-        names |= set(re.findall(r'getenv\("(MICSA_[A-Z_]+)"\)', open(f).read()))
-    doc = open(os.path.join(root, "INTEGRATION.md")).read()
-    short = set(re.findall(r"`_([A-Z]+)`", doc))  # the MICSA_SWEEP_* list written as `_PD`, ...
-    missing = [n for n in sorted(names)
-               if n not in doc and not (n.startswith("MICSA_SWEEP_") and n[12:] in short)]
-    assert names and not missing, missing
+    pkg = os.path.join(root, "micsa-ea-mc_gb300")
+    read = lambda fs: set().union(*(re.findall(r'getenv\("(MICSA_[A-Z_]+)"\)', open(f).read())
+                                    for f in fs))
+    drv = os.path.join(pkg, "host", "micsa_driver.c")
+    lib_names = read(glob.glob(os.path.join(pkg, "csrc", "*.cu")) +
+                     [f for f in glob.glob(os.path.join(pkg, "host", "*.c")) if f != drv])
+    drv_names = read([drv])
+    header = open(os.path.join(root, "include", "micsa.h")).read()
+    usage = open(drv).read().split("*/", 1)[0]
+    assert lib_names and drv_names
+    assert not [n for n in sorted(lib_names) if n not in header]
+    assert not [n for n in sorted(drv_names) if n not in usage]
