@@ -349,6 +349,19 @@ int micsa_set_active(micsa_ctx *ctx, const uint8_t *active);
 /* Wait for all work issued on the context (cudaDeviceSynchronize,
  * main.cu:144,149) and report any asynchronous error. */
 int micsa_synchronize(micsa_ctx *ctx);
+/* Test hook for the bounded device waits; no counterpart in the reference,
+ * whose failed CUDA calls exit (cudamacro.h:1-16).  The dataflow sweep
+ * (load=flow) orders its tiles by waiting on per-slab counters; each wait
+ * gives up after limit_ns nanoseconds of the GPU's global timer (0: the
+ * default, 2 s), after which every later wait of the launch gives up at
+ * once and micsa_synchronize reports the count as MICSA_ERR_CUDA (and
+ * clears it).  unreachable != 0 raises every wait's target beyond what the
+ * counters reach, so that every wait runs out: the iteration then completes
+ * without its ordering and its results are not valid.  The setting holds
+ * for every context on the device until changed; micsa_debug_flow_waits(ctx,
+ * 0, 0) restores operation.  Synchronises the context's stream. */
+int micsa_debug_flow_waits(micsa_ctx *ctx, uint64_t limit_ns, int unreachable);
+
 /* Number of kernels this context has launched so far (graph replays count
  * each kernel node). */
 int64_t micsa_kernel_launches(const micsa_ctx *ctx);

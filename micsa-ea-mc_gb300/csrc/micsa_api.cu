@@ -1134,7 +1134,23 @@ int micsa_synchronize(micsa_ctx *ctx) {
   MICSA_CK(micsa_tma_timeout_count(&to));
   if (to) return fail(ctx, MICSA_ERR_CUDA, "%u staged demon loads timed out (read directly)", to);
   MICSA_CK(micsa_flow_timeout_count(&to));
-  if (to) return fail(ctx, MICSA_ERR_CUDA, "%u waits of the dataflow sweep timed out", to);
+  if (to) {
+    /* reported once: cleared so that later launches wait again */
+    MICSA_CK(micsa_flow_timeout_clear());
+    return fail(ctx, MICSA_ERR_CUDA,
+                "%u waits of the dataflow sweep timed out: the results of that iteration are "
+                "not valid", to);
+  }
+  return MICSA_OK;
+}
+
+int micsa_debug_flow_waits(micsa_ctx *ctx, uint64_t limit_ns, int unreachable) {
+  if (!ctx) return MICSA_ERR_ARG;
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  MICSA_CK(cudaStreamSynchronize(ctx->stream));
+  MICSA_CK(micsa_flow_set_waits(limit_ns ? (unsigned long long)limit_ns : 2000000000ull,
+                                unreachable ? 0x40000000u : 0u, ctx->stream));
   return MICSA_OK;
 }
 

@@ -702,6 +702,11 @@ k_sweep(const micsa_geo g, const int p, const int ic, const int ytiles, const in
  * gives up at once, and micsa_flow_timeouts counts them); the last block to
  * finish resets the counters for the next launch. */
 __device__ unsigned int micsa_flow_timeouts;
+/* The wait limit, and an offset added to every wait's target count: 0 in
+ * operation; set through micsa_debug_flow_waits so that a test can make the
+ * waits run out (counters never reach a target raised by the offset). */
+__device__ unsigned long long micsa_flow_limit_ns = 2000000000ull;
+__device__ unsigned int micsa_flow_need_offset = 0u;
 
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *a) {
   unsigned v;
@@ -723,7 +728,7 @@ __device__ __forceinline__ bool flow_wait3(const unsigned *a, const unsigned *b,
     const unsigned x = ld_relaxed_u32(a), y = ld_relaxed_u32(b), z = ld_relaxed_u32(c);
     if (min(x, min(y, z)) >= need) break;
     if (!t0) t0 = global_ns();
-    if (*(volatile unsigned *)&micsa_flow_timeouts || global_ns() - t0 > 2000000000ull) {
+    if (*(volatile unsigned *)&micsa_flow_timeouts || global_ns() - t0 > micsa_flow_limit_ns) {
       ok = false;
       break;
     }
@@ -765,7 +770,7 @@ __device__ __forceinline__ void dep_take(const micsa_geo &g, const int *__restri
   if (j > 0 && !micsa_frozen(g, (int)s)) {
     const unsigned *c = ctl + 4 + s * nslab;
     if (!flow_wait3(c + (b == 0 ? nslab - 1 : b - 1), c + b, c + (b + 1 == nslab ? 0 : b + 1),
-                    T * j))
+                    T * j + micsa_flow_need_offset))
       atomicAdd(&micsa_flow_timeouts, 1u);
   }
 }
@@ -1768,6 +1773,22 @@ cudaError_t micsa_launch_sweep_flow(const micsa_geo &g, int sample_major, uint32
 
 cudaError_t micsa_flow_timeout_count(unsigned *n) {
   return cudaMemcpyFromSymbol(n, micsa_flow_timeouts, sizeof(unsigned));
+}
+
+cudaError_t micsa_flow_timeout_clear() {
+  const unsigned zero = 0;
+  return cudaMemcpyToSymbol(micsa_flow_timeouts, &zero, sizeof(unsigned));
+}
+
+cudaError_t micsa_flow_set_waits(unsigned long long limit_ns, unsigned need_offset,
+                                 cudaStream_t st) {
+  cudaError_t e = cudaMemcpyToSymbolAsync(micsa_flow_limit_ns, &limit_ns, sizeof limit_ns, 0,
+                                          cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyToSymbolAsync(micsa_flow_need_offset, &need_offset, sizeof need_offset, 0,
+                                cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st); /* the host values are on this stack */
+  return e;
 }
 
 cudaError_t micsa_make_tma(const micsa_geo &g, const uint32_t *d0, const uint32_t *d1,

@@ -86,6 +86,10 @@ cudaError_t micsa_launch_sweep_flow(const micsa_geo &g, int sample_major, uint32
                                     const int *walk, unsigned *ctl, cudaStream_t st);
 /* waits of the dataflow sweep that ran out since the process started */
 cudaError_t micsa_flow_timeout_count(unsigned *n);
+cudaError_t micsa_flow_timeout_clear();
+/* dataflow wait limit and target offset (0 in operation), see micsa_debug_flow_waits */
+cudaError_t micsa_flow_set_waits(unsigned long long limit_ns, unsigned need_offset,
+                                 cudaStream_t st);
 /* flag = 0 half-sweep of colour p with random words rnd[(k*P + i)*W + w] */
 cudaError_t micsa_launch_sweep_metropolis(const micsa_geo &g, int p,
                                           uint32_t *spin, const uint8_t *jb,

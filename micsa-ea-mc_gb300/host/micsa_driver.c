@@ -610,8 +610,14 @@ static void write_measures(unsigned long long ib, const int64_t *q, const int64_
       snprintf(name, sizeof name, "%sevol_xi.txt", dirsample[b]);
       if ((f = fopen(name, "a"))) {
         double x12, x23;
-        micsa_correlation_lengths(M.L, np, c4 + (int64_t)b * np * 3 * nd, NULL, &x12, &x23);
-        fprintf(f, "%llu %14.10g %14.10g\n", ib, x12, x23);
+        int rc;
+        micsa_correlation_lengths(M.L, np, c4 + (int64_t)b * np * 3 * nd, MICSA_XI_KAPPA, 0, NULL,
+                                  NULL, &x12, &x23, &rc);
+        if (ftell(f) == 0)
+          fprintf(f, "# t xi12 xi23 r_cut: integrals of C4(r) over r < r_cut, the first r >= 1 "
+                     "where C4(r) < %g x its standard error over the %d replica pairs\n",
+                  MICSA_XI_KAPPA, np);
+        fprintf(f, "%llu %14.10g %14.10g %d\n", ib, x12, x23, rc);
         fclose(f);
       }
     }

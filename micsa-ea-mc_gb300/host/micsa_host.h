@@ -163,10 +163,14 @@ void micsa_demon_stats(const uint64_t *e_demon, int nr, int L, int nc,
 
 /* ---- observables beyond the reference ----
  * c4[(k*3 + axis)*(L/2+1) + d] of npairs replica pairs (micsa_measure's
- * layout for one sample) -> C4r[d] (pair- and axis-averaged, / V; may be
- * NULL) and the integral-estimator correlation lengths xi12, xi23 */
-void micsa_correlation_lengths(int L, int npairs, const int64_t *c4, double *C4r,
-                               double *xi12, double *xi23);
+ * layout for one sample) -> C4r[d] (pair- and axis-averaged, / V), err[d]
+ * (its standard error over the pairs) and the integral-estimator
+ * correlation lengths xi12, xi23 summed over r < *rcut: the first r >= 1
+ * where C4r < kappa * err (kappa > 0), at most rmax + 1 (rmax > 0); kappa =
+ * rmax = 0 sums the whole range.  C4r, err and rcut may be NULL. */
+#define MICSA_XI_KAPPA 3.0 /* the cut-off the driver's evol_xi.txt uses */
+void micsa_correlation_lengths(int L, int npairs, const int64_t *c4, double kappa, int rmax,
+                               double *C4r, double *err, double *xi12, double *xi23, int *rcut);
 
 #ifdef __cplusplus
 }

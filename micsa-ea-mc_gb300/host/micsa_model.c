@@ -341,24 +341,49 @@ void micsa_demon_stats(const uint64_t *e_demon, int nr, int L, int nc,
 
 /* Correlation lengths from C4 by the integral estimators of the Janus
  * collaboration (Belletti et al., Phys. Rev. Lett. 101, 157201 (2008)):
- * I_k = sum_{r=0}^{L/2} r^k C4(r), xi_{k,k+1} = I_{k+1} / I_k, with C4(r)
- * the pair- and axis-averaged correlation normalised by V.  The sums run
- * over the whole range (no noise cut-off). */
-void micsa_correlation_lengths(int L, int npairs, const int64_t *c4, double *C4r,
-                               double *xi12, double *xi23) {
+ * I_k = sum_{r < r_cut} r^k C4(r), xi_{k,k+1} = I_{k+1} / I_k, with C4(r)
+ * the pair- and axis-averaged correlation normalised by V.  Far from the
+ * origin C4(r) is noise, and summing it with weights r^k swamps the
+ * estimate; the Janus analyses (Belletti et al., J. Stat. Phys. 135, 1121
+ * (2009)) therefore stop the integrals where C4 falls below a few times its
+ * statistical error.  Here the error of C4(r) is the standard error over the
+ * replica pairs (each pair's axis average is one estimate, pairs being
+ * independent), and r_cut is the first r >= 1 with C4(r) < kappa * err(r)
+ * (kappa > 0 and at least two pairs), capped at rmax + 1 when rmax > 0.
+ * kappa = 0 and rmax = 0 sum the whole range 0 .. L/2. */
+void micsa_correlation_lengths(int L, int npairs, const int64_t *c4, double kappa, int rmax,
+                               double *C4r, double *err, double *xi12, double *xi23, int *rcut) {
   const int nd = L / 2 + 1;
-  const double V = (double)L * L * L, norm = 1.0 / (V * 3.0 * (double)npairs);
+  const double V = (double)L * L * L;
+  int cut = nd;
+  if (rmax > 0 && rmax + 1 < cut) cut = rmax + 1;
   double I1 = 0, I2 = 0, I3 = 0;
   for (int d = 0; d < nd; d++) {
-    double s = 0;
-    for (int k = 0; k < npairs; k++)
-      for (int a = 0; a < 3; a++) s += (double)c4[((int64_t)k * 3 + a) * nd + d];
-    const double c = s * norm, r = (double)d;
+    double s = 0, s2 = 0;
+    for (int k = 0; k < npairs; k++) {
+      double pk = 0;
+      for (int a = 0; a < 3; a++) pk += (double)c4[((int64_t)k * 3 + a) * nd + d];
+      pk /= 3.0 * V;
+      s += pk;
+      s2 += pk * pk;
+    }
+    const double c = s / (double)npairs;
+    double e = 0;
+    if (npairs > 1) {
+      const double var = (s2 - s * c) / (double)(npairs - 1);
+      e = var > 0 ? sqrt(var / (double)npairs) : 0;
+    }
     if (C4r) C4r[d] = c;
-    I1 += r * c;
-    I2 += r * r * c;
-    I3 += r * r * r * c;
+    if (err) err[d] = e;
+    if (d >= 1 && d < cut && kappa > 0 && npairs > 1 && c < kappa * e) cut = d;
+    if (d < cut) {
+      const double r = (double)d;
+      I1 += r * c;
+      I2 += r * r * c;
+      I3 += r * r * r * c;
+    }
   }
+  if (rcut) *rcut = cut;
   if (xi12) *xi12 = I1 != 0 ? I2 / I1 : 0;
   if (xi23) *xi23 = I2 != 0 ? I3 / I2 : 0;
 }

@@ -14,6 +14,11 @@ LIB_PATH = os.path.join(PKG, "lib", "libmicsa.so")
 DRIVER_PATH = os.path.join(PKG, "bin", "micsa_run")
 
 MICSA_OK = 0
+MICSA_ERR_ARG = 1
+MICSA_ERR_CUDA = 2
+MICSA_ERR_NOMEM = 3
+MICSA_ERR_STATE = 4
+MICSA_ERR_UNSUPPORTED = 5
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE", 5: "ERR_UNSUPPORTED"}
 
 # symbols declared in include/micsa.h (checked by the CPU test suite)
@@ -27,6 +32,7 @@ ABI_SYMBOLS = [
     "micsa_synchronize", "micsa_kernel_launches", "micsa_stream", "micsa_job_measurements",
     "micsa_run_batch", "micsa_set_active", "micsa_serve", "micsa_job_beta",
     "micsa_server_create", "micsa_submit", "micsa_poll", "micsa_server_destroy",
+    "micsa_debug_flow_waits",
 ]
 NOALLOC_MAX_REPLICAS = 8192
 NOALLOC_MAX_L = 888
@@ -149,6 +155,7 @@ def lib():
         "micsa_stream": (C.c_void_p, [C.c_void_p]),
         "micsa_job_measurements": (C.c_int64, [C.c_int64]),
         "micsa_set_active": (C.c_int, [C.c_void_p, u8p]),
+        "micsa_debug_flow_waits": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int]),
         "micsa_job_beta": (C.c_double, [C.POINTER(Job), C.c_int64]),
         "micsa_serve": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(Request), C.c_int,
                                   C.POINTER(RequestResult), i32p, u64p, C.POINTER(C.c_double),
@@ -177,8 +184,10 @@ def lib():
                                             C.c_int, C.c_int, u64p, u64p, C.c_int]),
         "micsa_fill_bits": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), C.c_int, C.c_uint64,
                                    C.c_int, C.c_uint32, u32p]),
-        "micsa_correlation_lengths": (None, [C.c_int, C.c_int, i64p, C.POINTER(C.c_double),
-                                             C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "micsa_correlation_lengths": (None, [C.c_int, C.c_int, i64p, C.c_double, C.c_int,
+                                             C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                             C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                             C.POINTER(C.c_int)]),
         "micsa_draw_demons": (None, [C.POINTER(PRC), C.POINTER(Xoshiro), u64p, C.c_int, C.c_int,
                                      C.c_int, C.c_int, u64p, u64p]),
         # jump-ahead of the refresh streams (micsa-ea-mc_gb300/host/micsa_jump.h)
@@ -623,13 +632,23 @@ class Server:
             pass
 
 
-def correlation_lengths(L, c4):
+XI_KAPPA = 3.0  # the noise cut-off of the driver's evol_xi.txt
+
+
+def correlation_lengths(L, c4, kappa=0.0, rmax=0, with_cut=False):
     """(C4(r) averaged over pairs and axes / V, xi12, xi23) from one sample's
-    c4 array [pairs, 3, L/2+1] (micsa_measure's layout)."""
+    c4 array [pairs, 3, L/2+1] (micsa_measure's layout).  kappa > 0 stops the
+    integrals at the first r >= 1 where C4(r) < kappa x its standard error
+    over the pairs, rmax > 0 at r = rmax; with_cut=True also returns that
+    cut and the errors."""
     c = np.ascontiguousarray(c4, dtype=np.int64)
     npairs = c.size // (3 * (L // 2 + 1))
     out = np.zeros(L // 2 + 1, np.float64)
-    x12, x23 = C.c_double(), C.c_double()
-    lib().micsa_correlation_lengths(L, npairs, _ptr(c, C.c_int64), _ptr(out, C.c_double),
-                                    C.byref(x12), C.byref(x23))
+    err = np.zeros(L // 2 + 1, np.float64)
+    x12, x23, cut = C.c_double(), C.c_double(), C.c_int()
+    lib().micsa_correlation_lengths(L, npairs, _ptr(c, C.c_int64), kappa, rmax,
+                                    _ptr(out, C.c_double), _ptr(err, C.c_double), C.byref(x12),
+                                    C.byref(x23), C.byref(cut))
+    if with_cut:
+        return out, x12.value, x23.value, cut.value, err
     return out, x12.value, x23.value

@@ -89,7 +89,9 @@ def test_driver_observable_files(workdir):
         sd = os.path.join(workdir, "I000", "BIT%03d" % b)
         qlines = [l.split() for l in open(os.path.join(sd, "evol_q.txt"))]
         c4lines = [l.split() for l in open(os.path.join(sd, "evol_C4.txt"))]
-        xilines = [l.split() for l in open(os.path.join(sd, "evol_xi.txt"))]
+        xitext = open(os.path.join(sd, "evol_xi.txt")).read()
+        assert xitext.startswith("# t xi12 xi23 r_cut") and "standard error" in xitext
+        xilines = [l.split() for l in xitext.splitlines() if not l.startswith("#")]
         assert [int(l[0]) for l in qlines] == runs.measured(cfg)
         for k, t in enumerate(runs.measured(cfg)):
             uu = np.zeros((nr, V), np.uint8)
@@ -102,8 +104,9 @@ def test_driver_observable_files(workdir):
             assert [int(x) for x in qlines[k][1:]] == list(q), (b, t)
             got = {int(l[1]): int(l[2]) for l in c4lines if int(l[0]) == t}
             assert got == {d: int(c4[:, :, d].sum()) for d in range(nd)}, (b, t)
-            _, x12, x23 = micsa.correlation_lengths(L, c4)
-            assert xilines[k][0] == str(t)
+            _, x12, x23, cut, _ = micsa.correlation_lengths(L, c4, kappa=micsa.XI_KAPPA,
+                                                            with_cut=True)
+            assert xilines[k][0] == str(t) and int(xilines[k][3]) == cut
             assert abs(float(xilines[k][1]) - x12) <= 1e-9 * abs(x12) + 1e-12
             assert abs(float(xilines[k][2]) - x23) <= 1e-9 * abs(x23) + 1e-12
 

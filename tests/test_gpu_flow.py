@@ -113,3 +113,34 @@ def test_flow_sweep_headline_shape():
         ctx.iterate(2)
         ctx.synchronize()
         _check(ctx, st, L, nr, nc, 2)
+
+
+def test_dataflow_wait_that_runs_out_is_reported_and_the_gpu_stays_usable():
+    """The dataflow sweep's dependency waits are bounded.  With every wait's
+    target raised out of reach (a count nothing produces) and a 1 ms limit,
+    the first wait runs out, every later wait of the launch gives up at once,
+    the launch finishes, and micsa_synchronize turns the count into an error
+    with a message; nothing faults or hangs.  With the waits restored, a new
+    context on the same GPU runs bit-exact against the oracle."""
+    import torch
+    L, nr, nc, ns = 32, 64, 6, 2
+    st = random_state(np.random.default_rng(71), L, nr, nc, ns)
+    with _context(L, nr, ns, nc, zc=4, pd=2, occ=4) as ctx:
+        _upload(ctx, st)
+        lib = micsa.lib()
+        assert lib.micsa_debug_flow_waits(ctx.h, 1000000, 1) == micsa.MICSA_OK
+        try:
+            ctx.iterate(1)
+            rc = lib.micsa_synchronize(ctx.h)
+            msg = lib.micsa_last_error(ctx.h).decode()
+        finally:
+            assert lib.micsa_debug_flow_waits(ctx.h, 0, 0) == micsa.MICSA_OK
+        assert rc == micsa.MICSA_ERR_CUDA and "timed out" in msg, (rc, msg)
+        assert lib.micsa_synchronize(ctx.h) == micsa.MICSA_OK  # reported once, then cleared
+    torch.cuda.synchronize()  # the context of the device still answers
+    st = random_state(np.random.default_rng(72), L, nr, nc, ns)
+    with _context(L, nr, ns, nc, zc=4, pd=2, occ=4) as ctx:
+        _upload(ctx, st)
+        ctx.iterate(3)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, 3)
