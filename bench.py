@@ -58,6 +58,10 @@ def parse():
                     help="batched: one lattice size instead of the mixed-L stream")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="plain: leave out the compact batched and served results")
+    ap.add_argument("--extra-requests", type=int, default=60,
+                    help="plain: requests of the compact served result")
     a = ap.parse_args()
     if a.nsamples is None:
         a.nsamples = 512 if a.workload == "batched" else 2
@@ -442,6 +446,46 @@ def run_reference(a):
     return v, dt / a.steps * 1e3, threads
 
 
+def reference_cuda(a):
+    """The reference's own CUDA build on this GPU: its kernels
+    (d_oneMCstepBN_multisample, d_Walk; PROGRAM/src/main.cu compiled
+    unmodified for sm_103a by oracle/ref_gpu/build_ref_gpu.sh) launched as
+    Monte_Carlo launches them (main.cu:254-305: 2*nc sweeps and two walks per
+    iteration, calculate_blocks' geometry), on the same workload shape with a
+    seeded random reference-layout state, timed with CUDA events on the
+    harness's stream.  None where the cubin of this shape was not built."""
+    import oracle
+    cubin = oracle.ref_gpu_cubin(a.L, a.nr, max(2, a.nsamples))
+    if cubin is None:
+        return {"unavailable": "reference kernels for L=%d NR=%d not built here (they are compiled "
+                               "from the reference sources, absent where build() ran)" % (a.L, a.nr)}
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU"}
+    except Exception:
+        return {"unavailable": "no torch"}
+    st = cpu_state(a.L, a.nr, a.nsamples, a.nc, seed=11)
+    ref = oracle.RefGPU(cubin, a.L, a.nr, a.nsamples, a.nc)
+    try:
+        for s, (J, e, o, w0, w1) in enumerate(st):
+            ref.upload(s, J, e, o, w0, w1)
+        n = max(5, min(a.steps, 50))
+        ms = ref.time(max(3, a.warmup), n)
+        tpb, nb = ref.launch_shape()
+    finally:
+        ref.close()
+    attempts = float(a.L ** 3) * a.nr * a.nsamples * a.nc
+    return {"value": round(attempts / (ms * 1e9), 4), "unit": UNIT, "ms_per_step": round(ms, 4),
+            "steps": n, "kernels": "d_oneMCstepBN_multisample x %d + d_Walk x 2 per iteration"
+                                   % (2 * a.nc),
+            "launch": "grid (%d, %d) x %d threads" % (nb, a.nsamples, tpb),
+            "source": "the reference's PROGRAM/src/main.cu compiled unmodified for sm_103a "
+                      "(-DL=%d -DNBETAS=1 -DNUMBITSPREBUSQUEDAS=10 -DJANUS -DWALK, NR=%d, "
+                      "MAXNSAMPLES=%d), driven by oracle/ref_gpu/ref_gpu_harness.cu"
+                      % (a.L, a.nr, max(2, a.nsamples))}
+
+
 def config(a):
     return {"workload": "plain micSA, L=%d periodic +-J lattice, %d samples x %d replicas, "
                         "nc=%d demons/site; step = one iteration = %d half-sweeps + demon walk"
@@ -473,15 +517,16 @@ def batched_jobs(a):
                  beta=BETA) for L, it, (sj, su) in zip(Ls, its, seeds)]
 
 
-def run_batched(a, dist):
+def run_batched(a, dist, plain_sample=64):
     """All jobs through micsa_run_batch (host initialisation of the jobs
     outside the timed part; context creation, uploads, GPU refreshes,
-    iterations and measurement readbacks inside), against the plain path of
-    one micsa_run_batch call per job, timed on one job of every (L, sweeps)
-    pair and weighted by the pair counts.  Both sides are timed after a call
-    of every shape they use, so neither pays the launch-shape timing, which
-    the library does once per shape and process."""
-    import collections
+    iterations and measurement readbacks inside), against the plain path --
+    one micsa_run_batch call per job, the way one reference process runs one
+    sample -- measured on a seeded sample of `plain_sample` of the jobs (all
+    of them when plain_sample >= the job count), one call after another.
+    Both sides are timed after a call of every shape they use, so neither
+    pays the launch-shape timing, which the library does once per shape and
+    process."""
     import micsa
     jobs = batched_jobs(a)
     for w in range(max(0, a.warmup)):  # the first warm-up runs every job: every group shape
@@ -490,23 +535,31 @@ def run_batched(a, dist):
     es, ed, sec = micsa.run_batch(jobs, device=dist.local)
     sec = dist.max(sec)
     attempts = sum(float(j["L"] ** 3) * j["nr"] * j["nc"] * j["iterations"] for j in jobs)
-    count = collections.Counter((j["L"], j["iterations"]) for j in jobs)
-    plain, per = 0.0, {}
-    for L in sorted({k[0] for k in count}):  # launch shapes timed once per shape and process
+    for L in sorted({j["L"] for j in jobs}):  # launch shapes timed once per shape and process
         micsa.run_batch([dict(next(j for j in jobs if j["L"] == L), iterations=8)],
                         device=dist.local)
-    for key in sorted(count):
-        job = next(j for j in jobs if (j["L"], j["iterations"]) == key)
+    rng = np.random.default_rng(4242)
+    pick = (np.arange(len(jobs)) if plain_sample >= len(jobs)
+            else np.sort(rng.choice(len(jobs), size=plain_sample, replace=False)))
+    plain_attempts, plain_s = 0.0, 0.0
+    for k in pick:
+        job = jobs[int(k)]
         _, _, t1 = micsa.run_batch([job], device=dist.local)
-        per["L%d_%d" % key] = round(t1, 4)
-        plain += count[key] * t1
+        plain_s += t1
+        plain_attempts += float(job["L"] ** 3) * job["nr"] * job["nc"] * job["iterations"]
+    # the sample's measured time per attempt, applied to the whole stream
+    plain_total = plain_s * attempts / plain_attempts
     return {"anneals_per_s": round(len(jobs) * dist.world / sec, 2),
-            "plain_anneals_per_s": round(len(jobs) / plain, 2),
-            "speedup_vs_plain": round(plain / sec, 2),
+            "plain_anneals_per_s": round(len(jobs) / plain_total, 2),
+            "speedup_vs_plain": round(plain_total / sec, 2),
             "attempts_per_ps": round(attempts * dist.world / (sec * 1e12), 4),
-            "job_seconds": round(sec, 4), "plain_seconds_estimated": round(plain, 3),
-            "plain_seconds_per_job": per, "jobs": len(jobs),
-            "pairs": {"L%d_%d" % k: v for k, v in sorted(count.items())}}
+            "plain_attempts_per_ps": round(plain_attempts / (plain_s * 1e12), 4),
+            "job_seconds": round(sec, 4), "jobs": len(jobs),
+            "plain": "%d of the %d jobs (seeded sample) run one micsa_run_batch call each, one "
+                     "after another: %.3f s for %.3g attempts; the stream's plain time is that "
+                     "time per attempt x the stream's attempts" % (len(pick), len(jobs), plain_s,
+                                                                    plain_attempts),
+            "mode": os.environ.get("MICSA_BATCH", "groups")}
 
 
 SERVE_L = (16, 24, 32, 48, 64, 96)
@@ -527,47 +580,58 @@ def served_trace(a):
     return out
 
 
-def run_served(a, dist):
+def _replay_plain(reqs, device):
+    """The per-request path of the trace: one worker takes the requests in
+    arrival order, waits for each to arrive and runs it alone through
+    micsa_run_batch([job]) (host initialisation, context, uploads, refreshes,
+    iterations, measurements: one reference process per request).  Returns
+    the finish time of each request, seconds after the start."""
+    import micsa
+    t0 = time.perf_counter()
+    fin = []
+    for r in reqs:
+        wait = r["arrival"] - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        micsa.run_batch([r], device=device)
+        fin.append(time.perf_counter() - t0)
+    return np.array(fin)
+
+
+def run_served(a, dist, requests=None):
     """The trace through micsa_serve (continuous batching, HBM budget), in
-    real time; against the plain path: one micsa_run_batch call per request,
-    first come first served, service times from a per-(L, nr) linear fit of
-    single-job runs at 2^10 and 2^14 iterations."""
+    real time, against the plain path replayed in real time on the same GPU
+    after it: one request at a time, first come first served.  Both sides
+    are timed after a call of every shape they use (launch shapes are timed
+    once per shape and process)."""
     import micsa
     reqs = served_trace(a)
+    if requests is not None:
+        reqs = reqs[:requests]
     budget = int(a.hbm_gb * (1 << 30))
     micsa.serve([dict(r, arrival=0.0, iterations=8) for r in reqs[:6]], device=dist.local)
     es, ed, times, sec = micsa.serve(reqs, device=dist.local, hbm_budget=budget)
     lat = np.array([t[2] - r["arrival"] for t, r in zip(times, reqs)])
     wait = np.array([t[1] - r["arrival"] for t, r in zip(times, reqs)])
     attempts = sum(float(r["L"] ** 3) * r["nr"] * r["nc"] * r["iterations"] for r in reqs)
-    fit = {}
-    for L in SERVE_L:
-        for nr in (32, 64):
-            job = dict(L=L, nr=nr, nc=a.nc, seed_J=11, seed_u=13, beta=BETA)
-            micsa.run_batch([dict(job, iterations=8)], device=dist.local)  # shape timing
-            _, _, t1 = micsa.run_batch([dict(job, iterations=1 << 10)], device=dist.local)
-            _, _, t2 = micsa.run_batch([dict(job, iterations=1 << 14)], device=dist.local)
-            b = (t2 - t1) / ((1 << 14) - (1 << 10))
-            fit[(L, nr)] = (t1 - b * (1 << 10), b)
-    free_at, plat = 0.0, []
-    for r in reqs:
-        c0, c1 = fit[(r["L"], r["nr"])]
-        start = max(r["arrival"], free_at)
-        free_at = start + c0 + c1 * r["iterations"]
-        plat.append(free_at - r["arrival"])
-    plat = np.array(plat)
+    for shape in sorted({(r["L"], r["nr"]) for r in reqs}):
+        r0 = next(r for r in reqs if (r["L"], r["nr"]) == shape)
+        micsa.run_batch([dict(r0, iterations=8)], device=dist.local)
+    fin = _replay_plain(reqs, dist.local)
+    plat = fin - np.array([r["arrival"] for r in reqs])
     return {"anneals_per_s": round(len(reqs) / sec, 3),
             "p50_latency_s": round(float(np.percentile(lat, 50)), 3),
             "p99_latency_s": round(float(np.percentile(lat, 99)), 3),
             "p50_wait_s": round(float(np.percentile(wait, 50)), 3),
             "attempts_per_ps": round(attempts / (sec * 1e12), 4), "seconds": round(sec, 3),
-            "arrival_window_s": round(reqs[-1]["arrival"], 3),
-            "plain_anneals_per_s": round(len(reqs) / free_at, 3),
+            "arrival_window_s": round(reqs[-1]["arrival"], 3), "requests": len(reqs),
+            "plain_anneals_per_s": round(len(reqs) / float(fin[-1]), 3),
             "plain_p50_latency_s": round(float(np.percentile(plat, 50)), 3),
             "plain_p99_latency_s": round(float(np.percentile(plat, 99)), 3),
-            "speedup_vs_plain": round(free_at / sec, 2),
-            "plain_fit_s": {"L%d_nr%d" % k: [round(v[0], 4), round(v[1] * 1e6, 3)]
-                            for k, v in fit.items()},
+            "plain_seconds": round(float(fin[-1]), 3),
+            "speedup_vs_plain": round(float(fin[-1]) / sec, 2),
+            "plain": "measured: the same trace replayed in real time, one request at a time in "
+                     "arrival order, each through its own micsa_run_batch call",
             "hbm_budget_gib": a.hbm_gb}
 
 
@@ -642,6 +706,11 @@ def main():
                                                 % (a.nsamples, a.L, a.nr, a.nc)},
                      "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0,
                              "d2h_bytes_per_step": 0}})
+        if dist.world == 1:
+            try:
+                line["reference_cuda"] = reference_cuda(a)
+            except Exception as e:
+                line["reference_cuda"] = {"unavailable": str(e)[:300]}
         print(json.dumps(line))
         dist.close()
         return
@@ -651,9 +720,46 @@ def main():
                  "clocks": r["clocks"]})
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(a)
+    if dist.world == 1 and not a.no_extras:
+        line.update(extras(a, dist))
     if dist.rank == 0:
         print(json.dumps(line))
     dist.close()
+
+
+def extras(a, dist):
+    """The batched and served configurations, compactly, after the headline's
+    timed region: the full 512-job mixed-L batch against a measured sample of
+    48 of its jobs run one call each, and the first `--extra-requests` of the
+    served trace against the same requests replayed one at a time."""
+    import argparse
+    out = {}
+    b = argparse.Namespace(**vars(a))
+    b.nsamples, b.batch_L, b.nr, b.nc, b.warmup = 512, None, 64, 6, 1
+    try:
+        r = run_batched(b, dist, plain_sample=48)
+        out["batched"] = {k: r[k] for k in ("anneals_per_s", "plain_anneals_per_s",
+                                            "speedup_vs_plain", "attempts_per_ps", "job_seconds",
+                                            "jobs", "plain", "mode")}
+        out["batched"]["workload"] = ("512 jobs, L uniform in %s, sweeps uniform in %s, 64 "
+                                      "replicas, nc=6" % (list(BATCH_L), list(BATCH_SWEEPS)))
+    except Exception as e:  # the headline line is still printed
+        out["batched"] = {"error": str(e)[:300]}
+    c = argparse.Namespace(**vars(a))
+    c.nc = 6
+    try:
+        r = run_served(c, dist, requests=a.extra_requests)
+        out["served"] = {k: r[k] for k in (
+            "anneals_per_s", "p50_latency_s", "p99_latency_s", "plain_anneals_per_s",
+            "plain_p50_latency_s", "plain_p99_latency_s", "speedup_vs_plain", "attempts_per_ps",
+            "requests", "plain")}
+        out["served"]["workload"] = ("first %d requests of the Poisson trace (200/s, seed 7), L "
+                                     "uniform in %s, 32/64 replicas, sweeps log-uniform in "
+                                     "[2^10, 2^16], %g GiB HBM budget"
+                                     % (a.extra_requests, list(SERVE_L), a.hbm_gb))
+    except Exception as e:
+        out["served"] = {"error": str(e)[:300]}
+    return out
 
 
 if __name__ == "__main__":

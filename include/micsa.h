@@ -32,6 +32,10 @@
  *   MICSA_PDL=0          plain launches instead of programmatic dependent launch
  *   MICSA_REFRESH_WPS=n  segment length of the GPU demon refresh, in words
  *   MICSA_REFRESH_OCC=1  the refresh kernel without its register budget
+ *   MICSA_SWEEP_PF=n     the dataflow sweep requests n demon planes of each tile
+ *                        into L2 before its dependency wait
+ *   MICSA_MULTI_ZC=z     slab depth of the mixed-lattice launch (no timing)
+ *   MICSA_BATCH=groups|multi  how micsa_run_batch runs its shape groups
  * The command-line driver micsa_run adds MICSA_REFRESH=host,
  * MICSA_HOST_THREADS=n and MICSA_OBSERVABLES=1 (see its usage comment).
  */
@@ -337,6 +341,40 @@ int micsa_poll(micsa_server *sv, int64_t id, double timeout_s, int *done, int32_
 /* Let every submitted request finish, stop the threads and free the
  * contexts; results not yet polled are dropped.  NULL is accepted. */
 int micsa_server_destroy(micsa_server *sv);
+
+/* ---- Mixed-lattice launches: no counterpart in the reference ----
+ * One launch per iteration advances every running sample of several
+ * contexts -- of different L, with the same nr, on one device -- instead of
+ * one launch sequence per context: a dataflow sweep over a device work
+ * queue of (context, sample, half-sweep, slab, tile) tiles, each tile
+ * ordered after the half-sweep before it on its own and the neighbouring
+ * slabs, then the demon walks; replayed from a CUDA graph.  The reference
+ * runs one lattice shape per executable (header.h:20, main.cu:197-313).
+ * micsa_multi_create picks each context's slab depth and L2 prefetch
+ * distance and the launch's register budget and ticket order by timing
+ * whole iterations, which runs iterations on the contexts' buffers: create
+ * it before any state is uploaded (with state present the defaults are
+ * kept; MICSA_MULTI_ZC=z pins the slab depth where it divides L).  The
+ * choice is kept per process for the same list of shapes.  At most 16
+ * contexts.  The contexts stay usable as before (uploads, refreshes,
+ * measurements, run flags); micsa_multi_iterate is ordered after the work
+ * queued on every context's stream and before what is queued there next.
+ * Results equal micsa_iterate on each context alone.  err (optional)
+ * receives a message on failure. */
+typedef struct micsa_multi micsa_multi;
+int micsa_multi_create(micsa_ctx *const *ctxs, int n, micsa_multi **out, char *err,
+                       size_t errlen);
+/* n iterations of every running sample of every context (asynchronous);
+ * samples beyond a context's last running one take no tiles. */
+int micsa_multi_iterate(micsa_multi *m, int64_t n);
+/* wait for the launches and report a device error or timed-out waits */
+int micsa_multi_synchronize(micsa_multi *m);
+int micsa_multi_destroy(micsa_multi *m);
+const char *micsa_multi_last_error(const micsa_multi *m);
+int64_t micsa_multi_kernel_launches(const micsa_multi *m);
+/* "occ=<blocks per SM budget> smaj=<1: tiles sample-major> [cached] | L<L>:zc=<slab
+ * depth>,pd=<prefetch> ... | <candidate>:<ms per iteration> ..." */
+int micsa_multi_report(const micsa_multi *m, char *buf, size_t n);
 
 /* Per-sample run flags, active[s] != 0 = sample s runs (all, after
  * micsa_create; NULL restores that).  A frozen sample is skipped by the

@@ -15,6 +15,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <string>
 #include <thread>
 #include <tuple>
 #include <vector>
@@ -509,6 +510,13 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.flow = 0;
   g.quad = 0;
   {
+    /* MICSA_SWEEP_PF=n: the dataflow sweep requests n demon planes of each
+     * tile into L2 before its dependency wait (0: none) */
+    const char *e = getenv("MICSA_SWEEP_PF");
+    g.pf = e ? atoi(e) : 0;
+    if (g.pf < 0) g.pf = 0;
+  }
+  {
     /* MICSA_PDL=0: plain launches of the sweeps */
     const char *e = getenv("MICSA_PDL");
     g.pdl = !(e && !strcmp(e, "0"));
@@ -772,13 +780,22 @@ int refresh_into(micsa_ctx *ctx, int first, int count, void *prc, void *xo, cons
   micsa_xoshiro_t *X = (micsa_xoshiro_t *)xo;
   const int64_t nw = 2 * g.H * g.nc, nstreams = (int64_t)count * g.nr;
   const size_t words = (size_t)nstreams * MICSA_STREAM_REC;
-  /* segments of 48 words (3072 draws per lane) while that still gives 1024
-   * warps, else 32, else 16: each segment's start costs a fixed jump (about
-   * 17k instructions per lane), and small calls are latency-bound anyway --
-   * measured on GB300 over 8 ... 256 words for L = 16 ... 160.
-   * MICSA_REFRESH_WPS pins the length */
-  int wps = 48;
-  while (wps > 16 && (int64_t)count * g.W * ((nw + wps - 1) / wps) < 1024) wps -= 16;
+  /* Segment length in words (64 draws per lane each): each segment's start
+   * costs a fixed jump (about 17k instructions per lane), so long segments
+   * while enough warps remain -- the longest of 192 ... 64 words that still
+   * gives about four waves of the kernel's 12 resident warps per SM (7000
+   * warps); below that 48 words while that gives 1024 warps, else 32, else
+   * 16, since small calls are latency-bound.  Measured on GB300 over
+   * 8 ... 256 words for L = 16 ... 160 (L=160, 2 samples: 7.0 ms at 192
+   * words against 7.8 ms at 48).  MICSA_REFRESH_WPS pins the length. */
+  auto warps_at = [&](int w) { return (int64_t)count * g.W * ((nw + w - 1) / w); };
+  int wps = 0;
+  for (int w : {192, 128, 96, 64})
+    if (!wps && warps_at(w) >= 7000) wps = w;
+  if (!wps) {
+    wps = 48;
+    while (wps > 16 && warps_at(wps) < 1024) wps -= 16;
+  }
   if (const char *e = getenv("MICSA_REFRESH_WPS")) {
     const int v = atoi(e);
     if (v < 1 || v > 4096) return fail(ctx, MICSA_ERR_ARG, "MICSA_REFRESH_WPS=%s", e);
@@ -1151,6 +1168,404 @@ int micsa_debug_flow_waits(micsa_ctx *ctx, uint64_t limit_ns, int unreachable) {
   MICSA_CK(cudaStreamSynchronize(ctx->stream));
   MICSA_CK(micsa_flow_set_waits(limit_ns ? (unsigned long long)limit_ns : 2000000000ull,
                                 unreachable ? 0x40000000u : 0u, ctx->stream));
+  return MICSA_OK;
+}
+
+
+/* ------------------------------------------------ mixed-lattice launches */
+struct micsa_multi {
+  std::vector<micsa_ctx *> ctx;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  unsigned *ctl = nullptr;
+  size_t ctl_words = 0;
+  std::vector<int> zc, pd; /* per group */
+  int occ = 6, smaj = 1;
+  std::vector<unsigned> graph_ns; /* ns_run of each group in the captured graph */
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t graph_kernels = 0, launches = 0;
+  cudaEvent_t done = nullptr;
+  std::vector<cudaEvent_t> ev;
+  int cached = 0, tuned = 0;
+  std::string table; /* candidates timed */
+  char err[512] = {0};
+};
+
+namespace {
+
+int mfail(micsa_multi *m, int code, const char *fmt, ...) {
+  if (m) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(m->err, sizeof m->err, fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+#define MULTI_CK(call)                                                                 \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return mfail(m, MICSA_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                   __FILE__, __LINE__);                                                \
+  } while (0)
+
+/* the slab depth a group starts from: deep slabs at large L, more tiles at
+ * small L (every candidate divides L) */
+int multi_default_zc(int L) { return L % 8 == 0 && L >= 32 ? 8 : (L % 4 == 0 ? 4 : 2); }
+
+/* launch arguments for the groups' running prefixes ns[g] (0: the group
+ * takes no tickets) */
+int multi_args(micsa_multi *m, const std::vector<unsigned> &ns, micsa_multi_args *a) {
+  memset(a, 0, sizeof *a);
+  a->smaj = m->smaj;
+  unsigned first = 0, cnt = 0;
+  for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    if (!ns[gi]) continue;
+    const micsa_ctx *c = m->ctx[gi];
+    micsa_mgroup &x = a->gr[a->n++];
+    x.g = c->g;
+    x.spin = c->spin;
+    x.d0 = c->dem0;
+    x.d1 = c->dem1;
+    x.jb = c->jb;
+    x.walk = c->walk;
+    x.zc = m->zc[gi];
+    x.pd = m->pd[gi] < m->zc[gi] ? m->pd[gi] : 0;
+    x.nslab = (unsigned)(c->g.L / x.zc);
+    const int VW = c->g.W % 4 == 0 ? 4 : (c->g.W % 2 == 0 ? 2 : 1);
+    x.G = (unsigned)(c->g.W / VW);
+    const uint64_t units = (uint64_t)c->g.L * (c->g.Lh / 2) * x.G;
+    x.T = (unsigned)((units + MTPB - 1) / MTPB);
+    x.ns_run = ns[gi];
+    x.first = first;
+    x.cnt_off = cnt;
+    const uint64_t t = (uint64_t)ns[gi] * 2 * c->g.nc * x.nslab * x.T;
+    if (first + t >= (1ull << 31)) return mfail(m, MICSA_ERR_UNSUPPORTED, "more than 2^31 tiles");
+    first += (unsigned)t;
+    cnt += ns[gi] * x.nslab;
+  }
+  a->total = first;
+  a->ncnt = cnt;
+  if (4 + (size_t)cnt > m->ctl_words) return mfail(m, MICSA_ERR_STATE, "counter space");
+  return MICSA_OK;
+}
+
+/* one iteration of the groups' running prefixes, as a graph on m->stream */
+int multi_capture(micsa_multi *m, const std::vector<unsigned> &ns) {
+  if (m->exec) cudaGraphExecDestroy(m->exec);
+  if (m->graph) cudaGraphDestroy(m->graph);
+  m->exec = nullptr;
+  m->graph = nullptr;
+  micsa_multi_args a;
+  int rc = multi_args(m, ns, &a);
+  if (rc) return rc;
+  m->graph_ns = ns;
+  m->graph_kernels = a.n ? 2 : 0;
+  if (!a.n) return MICSA_OK;
+  MULTI_CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+  const cudaError_t le = micsa_launch_sweep_multi(a, m->occ, m->ctl, m->stream);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(m->stream, &graph);
+  if (le != cudaSuccess || ce != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return mfail(m, MICSA_ERR_CUDA, "capture of the mixed launch: %s",
+                 cudaGetErrorString(le != cudaSuccess ? le : ce));
+  }
+  m->graph = graph;
+  MULTI_CK(cudaGraphInstantiate(&m->exec, m->graph, 0));
+  return MICSA_OK;
+}
+
+std::vector<unsigned> multi_running(const micsa_multi *m) {
+  std::vector<unsigned> ns(m->ctx.size(), 0);
+  for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    const std::vector<uint8_t> &on = m->ctx[gi]->active_host;
+    for (int s = (int)on.size() - 1; s >= 0; s--)
+      if (on[s]) {
+        ns[gi] = (unsigned)s + 1;
+        break;
+      }
+  }
+  return ns;
+}
+
+/* mean ms of one iteration of all groups, the current shape */
+int multi_time(micsa_multi *m, double *ms) {
+  std::vector<unsigned> all(m->ctx.size());
+  for (size_t gi = 0; gi < m->ctx.size(); gi++) all[gi] = (unsigned)m->ctx[gi]->cfg.nsamples;
+  int rc = multi_capture(m, all);
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  MULTI_CK(cudaEventCreate(&e0));
+  MULTI_CK(cudaEventCreate(&e1));
+  for (int i = 0; i < 2; i++) MULTI_CK(cudaGraphLaunch(m->exec, m->stream));
+  const int reps = 6;
+  MULTI_CK(cudaEventRecord(e0, m->stream));
+  for (int i = 0; i < reps; i++) MULTI_CK(cudaGraphLaunch(m->exec, m->stream));
+  MULTI_CK(cudaEventRecord(e1, m->stream));
+  MULTI_CK(cudaEventSynchronize(e1));
+  float t = 0;
+  MULTI_CK(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t / reps;
+  return MICSA_OK;
+}
+
+struct multi_tune_entry {
+  std::vector<int> zc, pd;
+  int occ, smaj;
+  std::string table;
+};
+std::mutex multi_mu;
+std::map<std::vector<int>, multi_tune_entry> multi_cache;
+
+/* Shape of the mixed launch, by coordinate descent on whole-iteration
+ * timings (graph replays on the contexts' zeroed buffers): the register
+ * budget and ticket order first, then each group's slab depth and L2
+ * prefetch distance with the others held.  Kept per process by the list of
+ * (device, L, nr, samples, nc) of the groups. */
+int multi_tune(micsa_multi *m) {
+  std::vector<int> key = {m->device};
+  for (micsa_ctx *c : m->ctx) {
+    key.push_back(c->g.L);
+    key.push_back(c->cfg.nr);
+    key.push_back(c->cfg.nsamples);
+    key.push_back(c->g.nc);
+  }
+  const char *ec = getenv("MICSA_TUNE_CACHE");
+  const bool use_cache = !(ec && atoi(ec) == 0);
+  if (use_cache) {
+    std::lock_guard<std::mutex> lk(multi_mu);
+    auto it = multi_cache.find(key);
+    if (it != multi_cache.end()) {
+      m->zc = it->second.zc;
+      m->pd = it->second.pd;
+      m->occ = it->second.occ;
+      m->smaj = it->second.smaj;
+      m->table = it->second.table;
+      m->cached = 1;
+      return MICSA_OK;
+    }
+  }
+  char buf[96];
+  double best = 1e30, ms = 0;
+  int rc;
+  auto trial = [&](const char *what) -> int {
+    if ((rc = multi_time(m, &ms))) return rc;
+    snprintf(buf, sizeof buf, "%s:%.4fms ", what, ms);
+    m->table += buf;
+    return MICSA_OK;
+  };
+  if ((rc = trial("start"))) return rc;
+  best = ms;
+  const int occs[3] = {6, 5, 8};
+  int bo = m->occ;
+  const int W = m->ctx[0]->g.W;
+  for (int o : occs) {
+    if (o == m->occ || (o == 5 && W != 2)) continue;
+    m->occ = o;
+    snprintf(buf, sizeof buf, "occ=%d", o);
+    if ((rc = trial(buf))) return rc;
+    if (ms < best) best = ms, bo = o;
+  }
+  m->occ = bo;
+  m->smaj ^= 1;
+  if ((rc = trial(m->smaj ? "smaj=1" : "smaj=0"))) return rc;
+  if (ms < best) best = ms;
+  else m->smaj ^= 1;
+  for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    const int L = m->ctx[gi]->g.L;
+    int zs[8];
+    const int nz = micsa_sweep_zc_candidates(L, zs, 8);
+    int bz = m->zc[gi], bp = m->pd[gi];
+    for (int k = 0; k < nz; k++) {
+      if (zs[k] > 16 || L / zs[k] < 1) continue;
+      for (int pdv : {0, 2}) {
+        if ((zs[k] == bz && pdv == bp) || (pdv && zs[k] <= pdv)) continue;
+        m->zc[gi] = zs[k];
+        m->pd[gi] = pdv;
+        snprintf(buf, sizeof buf, "L%d/zc=%d/pd=%d", L, zs[k], pdv);
+        if ((rc = trial(buf))) return rc;
+        if (ms < best) best = ms, bz = zs[k], bp = pdv;
+      }
+    }
+    m->zc[gi] = bz;
+    m->pd[gi] = bp;
+  }
+  m->tuned = 1;
+  /* the timing ran iterations on the zeroed buffers: zero them again */
+  for (micsa_ctx *c : m->ctx) {
+    const micsa_geo &g = c->g;
+    const size_t sw = (size_t)c->cfg.nsamples * 2 * g.P * g.W;
+    const size_t dw = (size_t)c->cfg.nsamples * 2 * g.nc * g.P * g.W;
+    MULTI_CK(cudaMemsetAsync(c->spin, 0, 4 * sw, m->stream));
+    MULTI_CK(cudaMemsetAsync(c->dem0, 0, 4 * dw, m->stream));
+    MULTI_CK(cudaMemsetAsync(c->dem1, 0, 4 * dw, m->stream));
+    MULTI_CK(cudaMemsetAsync(c->walk, 0, sizeof(int) * c->cfg.nsamples, m->stream));
+  }
+  MULTI_CK(cudaStreamSynchronize(m->stream));
+  if (use_cache) {
+    multi_tune_entry t{m->zc, m->pd, m->occ, m->smaj, m->table};
+    std::lock_guard<std::mutex> lk(multi_mu);
+    multi_cache.emplace(key, std::move(t));
+  }
+  return MICSA_OK;
+}
+
+}  // namespace
+
+namespace {
+int multi_setup(micsa_multi *m, micsa_ctx *const *ctxs, int n);
+}
+
+int micsa_multi_create(micsa_ctx *const *ctxs, int n, micsa_multi **out, char *err,
+                       size_t errlen) {
+  if (err && errlen) err[0] = 0;
+  if (!out) return MICSA_ERR_ARG;
+  *out = nullptr;
+  if (!ctxs || n < 1 || n > MICSA_MULTI_MAX) {
+    if (err) snprintf(err, errlen, "need 1 to %d contexts, got %d", MICSA_MULTI_MAX, n);
+    return MICSA_ERR_ARG;
+  }
+  micsa_multi *m = new (std::nothrow) micsa_multi;
+  if (!m) return MICSA_ERR_NOMEM;
+  const int rc = multi_setup(m, ctxs, n);
+  if (rc) {
+    if (err) snprintf(err, errlen, "%s", m->err);
+    micsa_multi_destroy(m);
+    return rc;
+  }
+  *out = m;
+  return MICSA_OK;
+}
+
+namespace {
+int multi_setup(micsa_multi *m, micsa_ctx *const *ctxs, int n) {
+  bool fresh = true;
+  size_t words = 4;
+  for (int i = 0; i < n; i++) {
+    micsa_ctx *c = ctxs[i];
+    if (!c) return mfail(m, MICSA_ERR_ARG, "context %d is NULL", i);
+    for (int k = 0; k < i; k++)
+      if (ctxs[k] == c) return mfail(m, MICSA_ERR_ARG, "context %d given twice", i);
+    if (c->cfg.device != ctxs[0]->cfg.device)
+      return mfail(m, MICSA_ERR_ARG, "contexts on different devices");
+    if (c->g.W != ctxs[0]->g.W)
+      return mfail(m, MICSA_ERR_UNSUPPORTED, "contexts with different replica words (nr %d, %d)",
+                   ctxs[0]->cfg.nr, c->cfg.nr);
+    m->ctx.push_back(c);
+    m->zc.push_back(multi_default_zc(c->g.L));
+    m->pd.push_back(0);
+    words += (size_t)c->cfg.nsamples * c->g.L; /* slabs of depth >= 1 */
+    for (int s = 0; s < c->cfg.nsamples; s++)
+      if (c->have_spin[s] || c->have_dem[s]) fresh = false;
+  }
+  m->device = ctxs[0]->cfg.device;
+  MULTI_CK(cudaSetDevice(m->device));
+  int least = 0, greatest = 0;
+  MULTI_CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  MULTI_CK(cudaStreamCreateWithPriority(&m->stream, cudaStreamNonBlocking, greatest));
+  MULTI_CK(cudaMalloc(&m->ctl, 4 * words));
+  m->ctl_words = words;
+  MULTI_CK(cudaMemsetAsync(m->ctl, 0, 4 * words, m->stream));
+  MULTI_CK(cudaEventCreateWithFlags(&m->done, cudaEventDisableTiming));
+  m->ev.resize(n);
+  for (int i = 0; i < n; i++) MULTI_CK(cudaEventCreateWithFlags(&m->ev[i], cudaEventDisableTiming));
+  for (micsa_ctx *c : m->ctx) MULTI_CK(cudaStreamSynchronize(c->stream));
+  /* the shape is timed on buffers that hold no state yet; with state
+   * uploaded already, the defaults stand (the timing would advance it) */
+  if (const char *e = getenv("MICSA_MULTI_ZC")) {
+    const int z = atoi(e);
+    for (size_t gi = 0; gi < m->ctx.size(); gi++)
+      if (z > 0 && m->ctx[gi]->g.L % z == 0) m->zc[gi] = z;
+  } else if (fresh) {
+    int rc = multi_tune(m);
+    if (rc) return rc;
+  }
+  m->graph_ns.clear();
+  return MICSA_OK;
+}
+}  // namespace
+
+int micsa_multi_destroy(micsa_multi *m) {
+  if (!m) return MICSA_OK;
+  if (m->stream) {
+    cudaSetDevice(m->device);
+    cudaStreamSynchronize(m->stream);
+  }
+  if (m->exec) cudaGraphExecDestroy(m->exec);
+  if (m->graph) cudaGraphDestroy(m->graph);
+  if (m->ctl) cudaFree(m->ctl);
+  if (m->done) cudaEventDestroy(m->done);
+  for (cudaEvent_t e : m->ev)
+    if (e) cudaEventDestroy(e);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+  return MICSA_OK;
+}
+
+const char *micsa_multi_last_error(const micsa_multi *m) { return m ? m->err : "null handle"; }
+
+int micsa_multi_iterate(micsa_multi *m, int64_t n) {
+  if (!m || n < 0) return mfail(m, MICSA_ERR_ARG, "bad argument");
+  MULTI_CK(cudaSetDevice(m->device));
+  for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    micsa_ctx *c = m->ctx[gi];
+    if (ready_for_sweeps(c, 1)) return mfail(m, MICSA_ERR_STATE, "group %zu: %s", gi, c->err);
+  }
+  const std::vector<unsigned> ns = multi_running(m);
+  bool any = false;
+  for (unsigned v : ns) any |= v > 0;
+  if (!any || n == 0) return MICSA_OK;
+  if (!m->exec || ns != m->graph_ns) {
+    const int rc = multi_capture(m, ns);
+    if (rc) return rc;
+  }
+  /* ordered after the work queued on every group's stream, and before what
+   * is queued there next */
+  for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    MULTI_CK(cudaEventRecord(m->ev[gi], m->ctx[gi]->stream));
+    MULTI_CK(cudaStreamWaitEvent(m->stream, m->ev[gi], 0));
+  }
+  for (int64_t i = 0; i < n; i++) MULTI_CK(cudaGraphLaunch(m->exec, m->stream));
+  m->launches += n * m->graph_kernels;
+  MULTI_CK(cudaEventRecord(m->done, m->stream));
+  for (micsa_ctx *c : m->ctx) MULTI_CK(cudaStreamWaitEvent(c->stream, m->done, 0));
+  return MICSA_OK;
+}
+
+int micsa_multi_synchronize(micsa_multi *m) {
+  if (!m) return MICSA_ERR_ARG;
+  MULTI_CK(cudaSetDevice(m->device));
+  MULTI_CK(cudaStreamSynchronize(m->stream));
+  MULTI_CK(cudaGetLastError());
+  unsigned to = 0;
+  MULTI_CK(micsa_flow_timeout_count(&to));
+  if (to) {
+    MULTI_CK(micsa_flow_timeout_clear());
+    return mfail(m, MICSA_ERR_CUDA, "%u waits of the mixed dataflow sweep timed out", to);
+  }
+  return MICSA_OK;
+}
+
+int64_t micsa_multi_kernel_launches(const micsa_multi *m) { return m ? m->launches : 0; }
+
+int micsa_multi_report(const micsa_multi *m, char *buf, size_t n) {
+  if (!m || !buf || !n) return MICSA_ERR_ARG;
+  std::string s;
+  char t[96];
+  snprintf(t, sizeof t, "occ=%d smaj=%d%s |", m->occ, m->smaj, m->cached ? " cached" : "");
+  s += t;
+  for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    snprintf(t, sizeof t, " L%d:zc=%d,pd=%d", m->ctx[gi]->g.L, m->zc[gi], m->pd[gi]);
+    s += t;
+  }
+  s += " | ";
+  s += m->table;
+  snprintf(buf, n, "%s", s.c_str());
   return MICSA_OK;
 }
 

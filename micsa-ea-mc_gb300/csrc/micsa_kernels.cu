@@ -389,7 +389,10 @@ __device__ __forceinline__ void st_u32(uint32_t *a, uint32_t v, uint64_t pol) {
  * `tile`, x block bx, z planes [z0, z0 + zc), demon walk kwalk.  FLOW: the
  * other colour is read through the coherent path (other tiles of the same
  * dataflow launch write it). */
-template <int VW, bool MICSA, bool WIDE, bool TMA, bool FLOW, int S = 2>
+/* LIN: the thread's row and x/2 pair come from the caller (tile = y,
+ * bx = pair index), not from the block shape -- the mixed-lattice launch
+ * maps a fixed block onto consecutive (row, pair) units of any L. */
+template <int VW, bool MICSA, bool WIDE, bool TMA, bool FLOW, int S = 2, bool LIN = false>
 __device__ __forceinline__ void sweep_block(
     const micsa_geo &g, const int p, const int ic, const uint32_t s, const uint32_t grp,
     const uint32_t tile, const uint32_t bx, const uint32_t z0, const int zc, const int pd,
@@ -397,12 +400,13 @@ __device__ __forceinline__ void sweep_block(
     uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb, const uint32_t *__restrict__ rnd,
     const micsa_tma &tm) {
   static_assert(S == 2 || (S == 4 && VW == 1 && WIDE && !TMA), "four sites: one word each");
+  static_assert(!(LIN && TMA), "TMA staging needs the block-shaped tile");
   constexpr int N = S * VW; /* words per thread and plane */
   using PR = typename sites_io<VW, WIDE, S>::type;
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
-  const uint32_t y = tile * blockDim.y + threadIdx.y;
+  const uint32_t y = LIN ? tile : tile * blockDim.y + threadIdx.y;
   if (y >= L) return;
-  const uint32_t xa = S * (bx * blockDim.x + threadIdx.x); /* x/2 of the first site */
+  const uint32_t xa = S * (LIN ? bx : bx * blockDim.x + threadIdx.x); /* x/2 of the first site */
   const uint32_t plane = L * Lh;
   const uint32_t row = y * Lh + xa;
   const uint32_t rowN = (y + 1 == L) ? xa : row + Lh;
@@ -767,11 +771,54 @@ __device__ __forceinline__ void dep_take(const micsa_geo &g, const int *__restri
   job[4] = (t / gx) % ytiles;
   job[5] = t / (gx * ytiles);
   job[6] = (unsigned)__ldg(walk + s);
+}
+/* ... and the lead thread's wait for the tile's dependencies */
+__device__ __forceinline__ void dep_wait(const micsa_geo &g, unsigned *__restrict__ ctl,
+                                         const unsigned *cst, const unsigned *job) {
+  const unsigned s = job[0], j = job[1], b = job[2], nslab = cst[C_NSLAB], T = cst[C_T];
   if (j > 0 && !micsa_frozen(g, (int)s)) {
     const unsigned *c = ctl + 4 + s * nslab;
     if (!flow_wait3(c + (b == 0 ? nslab - 1 : b - 1), c + b, c + (b + 1 == nslab ? 0 : b + 1),
                     T * j + micsa_flow_need_offset))
       atomicAdd(&micsa_flow_timeouts, 1u);
+  }
+}
+
+/* L2 prefetch of the demon words a thread of a sweep_block tile will read:
+ * plane (p, ic) of sample s, rows as sweep_block derives them, z planes
+ * [z0, z0 + n).  The demon planes are read and written by one half-sweep
+ * only, so a dataflow tile can request them before its dependency wait. */
+template <int VW>
+__device__ __forceinline__ void prefetch_tile_demons(const micsa_geo &g, int p, int ic,
+                                                     uint32_t s, uint32_t grp, uint32_t tile,
+                                                     uint32_t bx, uint32_t z0, int n, int kwalk,
+                                                     const uint32_t *d0, const uint32_t *d1) {
+  const uint32_t L = g.L, Lh = g.Lh, W = g.W;
+  const uint32_t y = tile * blockDim.y + threadIdx.y;
+  if (y >= L) return;
+  const uint32_t xa = 2 * (bx * blockDim.x + threadIdx.x);
+  const int sh = ((p == 0) == (ic < 3)) ? kwalk : -kwalk;
+  const int axis = ic < 3 ? ic : ic - 3;
+  uint32_t drow = y * Lh + xa, zd = z0;
+  if (axis == 0) {
+    int xd = (int)xa - sh;
+    xd += xd < 0 ? (int)Lh : (xd >= (int)Lh ? -(int)Lh : 0);
+    drow = y * Lh + (uint32_t)xd;
+  } else if (axis == 1) {
+    int yd = (int)y - 2 * sh;
+    yd += yd < 0 ? (int)L : (yd >= (int)L ? -(int)L : 0);
+    drow = (uint32_t)yd * Lh + xa;
+  } else {
+    int t = (int)z0 - 2 * sh;
+    t += t < 0 ? (int)L : (t >= (int)L ? -(int)L : 0);
+    zd = (uint32_t)t;
+  }
+  const size_t base = ((size_t)(s * 2 + p) * g.nc + ic) * (size_t)g.P * W + grp * VW;
+  const uint32_t plane = L * Lh;
+  for (int t = 0; t < n; t++) {
+    prefetch_l2(d0 + base + (size_t)(zd * plane + drow) * W);
+    prefetch_l2(d1 + base + (size_t)(zd * plane + drow) * W);
+    zd = (zd + 1 == L) ? 0 : zd + 1;
   }
 }
 
@@ -781,7 +828,8 @@ __device__ __forceinline__ void dep_take(const micsa_geo &g, const int *__restri
 template <int VW, bool WIDE, int MINB>
 __global__ void __launch_bounds__(TPB, MINB)
 k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, const int zc,
-            const int pd, const int smaj, uint32_t *__restrict__ spin, uint32_t *__restrict__ d0,
+            const int pd, const int smaj, const int pf, uint32_t *__restrict__ spin,
+            uint32_t *__restrict__ d0,
             uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
             const int *__restrict__ walk, unsigned *__restrict__ ctl) {
   grid_dependency_sync();
@@ -801,6 +849,15 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
     cst[C_SMAJ] = (unsigned)smaj;
     dep_take(g, walk, ctl, cst, job);
   }
+  __syncthreads();
+  /* the tile's demon words are independent of the half-sweep before it:
+   * on their way into L2 while the lead thread waits for the dependencies
+   * (at most pf planes: the z loop's own prefetch takes over from there) */
+  if (pf > 0 && !micsa_frozen(g, (int)job[0]))
+    prefetch_tile_demons<VW>(g, (int)(job[1] & 1u), (int)(job[1] >> 1), job[0], job[5], job[4],
+                             job[3], job[2] * (unsigned)zc, pf < zc ? pf : zc, (int)job[6], d0,
+                             d1);
+  if (lead) dep_wait(g, ctl, cst, job);
   __syncthreads();
   {
     const unsigned s = job[0], j = job[1];
@@ -824,6 +881,102 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
     const unsigned n = (unsigned)g.ns * cst[C_NSLAB];
     for (unsigned k = tid; k < n; k += nt) ctl[4 + k] = 0;
     if (lead) {
+      ctl[0] = 0;
+      ctl[1] = 0;
+    }
+  }
+}
+
+/* ------------------------------------------ mixed-lattice dataflow sweep */
+/* One launch advances every sample of several contexts (groups) of
+ * different L by one iteration: the dataflow sweep above, generalised to a
+ * table of groups.  A ticket u falls in group gi when first[gi] <= u <
+ * first[gi + 1]; inside the group it is decoded as in k_sweep_dep (sample,
+ * half-sweep j, slab, tile; sample-major or half-sweep-major), and a tile of
+ * half-sweep j on slab b waits until j-1 has finished slabs b-1, b, b+1 of
+ * the same sample (the group's own counters).  The block is a fixed MTPB
+ * threads mapped onto consecutive (word group, row, x/2 pair) units of the
+ * slab -- rows of a z plane are contiguous, so a block's loads stay
+ * coalesced at any L -- and each thread marches the group's zc planes.
+ * Tickets are only taken for samples [0, ns_run) of each group (the
+ * running prefix); frozen samples inside it are skipped. */
+__global__ void __launch_bounds__(MTPB, 8)
+k_walk_multi(const __grid_constant__ micsa_multi_args a) {
+  const int gi = blockIdx.y, s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= a.n) return;
+  const micsa_mgroup &m = a.gr[gi];
+  if (s < (int)m.ns_run && !micsa_frozen(m.g, s)) {
+    int *w = m.walk + s;
+    const int k = *w + 1;
+    *w = (k == m.g.L / 2) ? 0 : k;
+  }
+}
+
+template <int VW, bool WIDE, int MINB>
+__global__ void __launch_bounds__(MTPB, MINB)
+k_sweep_multi(const __grid_constant__ micsa_multi_args a, unsigned *__restrict__ ctl) {
+  grid_dependency_sync();
+  __shared__ unsigned job[8]; /* group, s, j, slab, tile, walk, last */
+  /* the tile's group, copied out of the parameter table: read from shared
+   * memory where used, so that none of it occupies registers */
+  __shared__ micsa_mgroup m;
+  if (threadIdx.x == 0) {
+    const unsigned u = atomicAdd(ctl, 1u);
+    int gi = 0;
+    while (gi + 1 < a.n && u >= a.gr[gi + 1].first) gi++;
+    m = a.gr[gi];
+    const unsigned r = u - m.first, per_half = m.nslab * m.T;
+    unsigned s, j, r2;
+    if (a.smaj) {
+      const unsigned per_sample = 2u * (unsigned)m.g.nc * per_half;
+      s = r / per_sample;
+      j = (r % per_sample) / per_half;
+      r2 = r % per_half;
+    } else {
+      const unsigned per_j = m.ns_run * per_half;
+      j = r / per_j;
+      s = (r % per_j) / per_half;
+      r2 = r % per_half;
+    }
+    const unsigned b = (r2 / m.T + j) % m.nslab;
+    job[0] = (unsigned)gi;
+    job[1] = s;
+    job[2] = j;
+    job[3] = b;
+    job[4] = r2 % m.T;
+    job[5] = (unsigned)__ldg(m.walk + s);
+    if (j > 0 && !micsa_frozen(m.g, (int)s)) {
+      const unsigned *c = ctl + 4 + m.cnt_off + s * m.nslab;
+      if (!flow_wait3(c + (b == 0 ? m.nslab - 1 : b - 1), c + b,
+                      c + (b + 1 == m.nslab ? 0 : b + 1), m.T * j + micsa_flow_need_offset))
+        atomicAdd(&micsa_flow_timeouts, 1u);
+    }
+  }
+  __syncthreads();
+  {
+    const unsigned s = job[1], j = job[2];
+    const unsigned v = job[4] * MTPB + threadIdx.x; /* unit of the slab: (grp, row, pair) */
+    const unsigned pairs = (unsigned)m.g.Lh / 2u, units = (unsigned)m.g.L * pairs;
+    if (!micsa_frozen(m.g, (int)s) && v < units * m.G) {
+      const unsigned grp = v / units, w = v % units;
+      micsa_tma none;
+      sweep_block<VW, true, WIDE, false, true, 2, true>(
+          m.g, (int)(j & 1u), (int)(j >> 1), s, grp, w / pairs, w % pairs,
+          job[3] * (unsigned)m.zc, m.zc, m.pd, (int)job[5], m.spin, m.d0, m.d1, m.jb, nullptr,
+          none);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(ctl + 4 + m.cnt_off + job[1] * m.nslab + job[3], 1u);
+    __threadfence();
+    job[6] = atomicAdd(ctl + 1, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (job[6]) { /* every other block has finished: reset for the next launch */
+    for (unsigned k = threadIdx.x; k < a.ncnt; k += MTPB) ctl[4 + k] = 0;
+    if (threadIdx.x == 0) {
       ctl[0] = 0;
       ctl[1] = 0;
     }
@@ -1733,7 +1886,7 @@ static cudaError_t sweep_flow_k(const micsa_geo &g, int smaj, int ytiles, int G,
                                 uint32_t *d1, const uint8_t *jb, const int *walk, unsigned *ctl,
                                 cudaStream_t st) {
   return launch_sweep(g, k_sweep_dep<VW, WIDE, MINB>, dim3((unsigned)tiles), block, 0, st, g,
-                      ytiles, G, zc, g.pd, smaj, spin, d0, d1, jb, walk, ctl);
+                      ytiles, G, zc, g.pd, smaj, g.pf, spin, d0, d1, jb, walk, ctl);
 }
 
 template <int VW>
@@ -2019,6 +2172,22 @@ k_refresh(const micsa_geo g, const int first, const int count, const int64_t nwo
   const int64_t i0 = seg * wps;
   const int64_t i1 = i0 + wps < nwords ? i0 + wps : nwords;
   const int sample = first + j;
+  /* Where the two sites of this lane's bits (lane, lane + 32) of word i live
+   * at walk 0: word i = pi*H + h is colour p = pi / nc, plane ic = pi % nc,
+   * MSC word h = a2 + mh*(bb + m*c); the site of bit b is x = (b&3)*m + a
+   * (a = 2*a2 + parity, so x/2 = (b&3)*mh + a2), y = ((b>>2)&3)*m + bb,
+   * z = (b>>4)*m + c (ini.c:317-337), stored at (z*L + y)*Lh + x/2.  That
+   * splits into a lane part and a warp-uniform word part, the latter
+   * stepped along with i instead of divided out per word. */
+  const int m = g.L >> 2, mh = m >> 1;
+  const int64_t slab = (int64_t)m * g.L * g.Lh; /* one block step in z */
+  const int64_t lane_a = ((int64_t)(lane >> 4) * slab) + (int64_t)((lane >> 2) & 3) * m * g.Lh +
+                         (int64_t)(lane & 3) * mh;
+  const int64_t lane_b = lane_a + 2 * slab;
+  int64_t pi = i0 / g.H;
+  int64_t hrem = i0 % g.H;
+  int a2 = (int)(hrem % mh), bb = (int)((hrem / mh) % m), c = (int)(hrem / ((int64_t)mh * m));
+  int64_t base = ((int64_t)sample * 2 * g.nc + pi) * g.P * g.W + w;
   for (int64_t i = i0; i < i1; i++) {
     uint64_t d0 = 0, d1 = 0;
 #pragma unroll
@@ -2034,20 +2203,27 @@ k_refresh(const micsa_geo g, const int first, const int count, const int64_t nwo
       d0 |= (uint64_t)(a0 ^ a1 ^ a2) << b;
       d1 |= (uint64_t)((a0 & a1) | (a0 & a2) | (a1 & a2)) << b;
     }
-    const int64_t pi = i / g.H, h = i % g.H;
-    const int p = (int)(pi / g.nc), ic = (int)(pi % g.nc);
     const uint32_t lo0 = warp_transpose32((uint32_t)d0, lane);
     const uint32_t hi0 = warp_transpose32((uint32_t)(d0 >> 32), lane);
     const uint32_t lo1 = warp_transpose32((uint32_t)d1, lane);
     const uint32_t hi1 = warp_transpose32((uint32_t)(d1 >> 32), lane);
-    const site_xyz sa = ref_site(g, p, h, lane), sb = ref_site(g, p, h, lane + 32);
-    const int64_t base = ((int64_t)sample * 2 * g.nc + pi) * g.P * g.W + w;
-    const int64_t oa = base + demon_slot(g, p, ic, 0, sa.x, sa.y, sa.z) * g.W;
-    const int64_t ob = base + demon_slot(g, p, ic, 0, sb.x, sb.y, sb.z) * g.W;
+    const int64_t word = ((int64_t)c * g.L + bb) * g.Lh + a2;
+    const int64_t oa = base + (word + lane_a) * g.W;
+    const int64_t ob = base + (word + lane_b) * g.W;
     dem0[oa] = lo0;
     dem0[ob] = hi0;
     dem1[oa] = lo1;
     dem1[ob] = hi1;
+    if (++a2 == mh) {
+      a2 = 0;
+      if (++bb == m) {
+        bb = 0;
+        if (++c == m) { /* next (colour, plane) */
+          c = 0;
+          base += g.P * g.W;
+        }
+      }
+    }
   }
 }
 
@@ -2186,6 +2362,38 @@ cudaError_t micsa_launch_resident(const micsa_geo &g, int n, uint32_t *spin, uin
   if (g.L == 8) return resident_l<8>(g, n, spin, d0, d1, jb, walk, st);
   if (g.L == 16) return resident_l<16>(g, n, spin, d0, d1, jb, walk, st);
   return cudaErrorInvalidValue;
+}
+
+cudaError_t micsa_launch_sweep_multi(const micsa_multi_args &a, int occ, unsigned *ctl,
+                                     cudaStream_t st) {
+  if (a.n < 1 || a.n > MICSA_MULTI_MAX || a.total == 0) return cudaErrorInvalidValue;
+  const int W = a.gr[0].g.W;
+  for (int i = 1; i < a.n; i++)
+    if (a.gr[i].g.W != W) return cudaErrorInvalidValue;
+  const dim3 grid(a.total), block(MTPB);
+  /* the word vector of one site: 4, 2 or 1 words; one group of them (WIDE)
+   * when it is all of a site's words */
+  if (W % 4 == 0) {
+    if (W == 4) k_sweep_multi<4, true, 4><<<grid, block, 0, st>>>(a, ctl);
+    else k_sweep_multi<4, false, 4><<<grid, block, 0, st>>>(a, ctl);
+  } else if (W % 2 == 0) {
+    if (W == 2) {
+      if (occ == 8) k_sweep_multi<2, true, 8><<<grid, block, 0, st>>>(a, ctl);
+      else if (occ == 5) k_sweep_multi<2, true, 5><<<grid, block, 0, st>>>(a, ctl);
+      else k_sweep_multi<2, true, 6><<<grid, block, 0, st>>>(a, ctl);
+    } else {
+      k_sweep_multi<2, false, 6><<<grid, block, 0, st>>>(a, ctl);
+    }
+  } else {
+    if (occ == 8) k_sweep_multi<1, true, 8><<<grid, block, 0, st>>>(a, ctl);
+    else k_sweep_multi<1, true, 6><<<grid, block, 0, st>>>(a, ctl);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  unsigned maxns = 1;
+  for (int i = 0; i < a.n; i++) maxns = a.gr[i].ns_run > maxns ? a.gr[i].ns_run : maxns;
+  k_walk_multi<<<dim3((maxns + MTPB - 1) / MTPB, a.n), MTPB, 0, st>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t micsa_tma_timeout_count(unsigned *n) {

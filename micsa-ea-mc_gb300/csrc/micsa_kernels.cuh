@@ -37,6 +37,8 @@ struct micsa_geo {
   int tw;     /* 1: sweep blocks span whole rows along x (when that differs) */
   int flow;   /* 1: an iteration's half-sweeps run as one dataflow launch */
   int quad;   /* 1: four one-word sites per sweep thread (W = 1, direct loads) */
+  int pf;     /* dataflow sweep: demon planes of its tile requested into L2 before its
+                 dependency wait (0 = none) */
   int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */
@@ -84,6 +86,35 @@ cudaError_t micsa_launch_sweep_micsa(const micsa_geo &g, int p, int ic,
 cudaError_t micsa_launch_sweep_flow(const micsa_geo &g, int sample_major, uint32_t *spin,
                                     uint32_t *d0, uint32_t *d1, const uint8_t *jb,
                                     const int *walk, unsigned *ctl, cudaStream_t st);
+/* Mixed-lattice dataflow sweep: one launch advances every running sample of
+ * up to MICSA_MULTI_MAX groups (contexts, possibly of different L, same W)
+ * by one iteration, then their demon walks.  Block of MTPB threads over
+ * consecutive (word group, row, x/2 pair) units of a slab. */
+#define MICSA_MULTI_MAX 16
+constexpr int MTPB = 128;
+struct micsa_mgroup {
+  micsa_geo g;               /* the group's geometry (active flags included) */
+  uint32_t *spin, *d0, *d1;  /* the group's device state */
+  const uint8_t *jb;
+  int *walk;
+  unsigned first;            /* first ticket of the group */
+  unsigned ns_run;           /* samples [0, ns_run) take tickets */
+  unsigned cnt_off;          /* the group's [ns_run][nslab] counters start at ctl[4 + cnt_off] */
+  unsigned nslab, T;         /* slabs (L/zc) and tiles per slab */
+  unsigned G;                /* word groups per site, W / VW */
+  int zc, pd;                /* slab depth, L2 prefetch distance */
+};
+struct micsa_multi_args {
+  int n;                     /* groups */
+  int smaj;                  /* 1: tickets sample-major within a group, 0: half-sweep-major */
+  unsigned total;            /* tickets = blocks */
+  unsigned ncnt;             /* counter words after the 4 header words */
+  micsa_mgroup gr[MICSA_MULTI_MAX];
+};
+/* occ: blocks per SM the registers are budgeted for: 8 (64 registers), 5
+ * (96, two-word sites only) or 6 (80, the default) */
+cudaError_t micsa_launch_sweep_multi(const micsa_multi_args &a, int occ, unsigned *ctl,
+                                     cudaStream_t st);
 /* waits of the dataflow sweep that ran out since the process started */
 cudaError_t micsa_flow_timeout_count(unsigned *n);
 cudaError_t micsa_flow_timeout_clear();

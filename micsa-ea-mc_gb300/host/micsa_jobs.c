@@ -9,6 +9,7 @@
  * numbers equal those of the same job run alone.
  */
 #include <pthread.h>
+#include <stdint.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -117,106 +118,239 @@ typedef struct {
   uint64_t *e_demon;
   int rc;
   char err[256];
+  /* run state */
+  micsa_prc_t *gprc;     /* [n][nr] the slots' streams */
+  micsa_xoshiro_t *gxo;
+  int32_t *es;
+  uint64_t *ed;
+  uint8_t *on;
+  int64_t *m;            /* measurements written per slot */
+  int nrun;
+  uint64_t thr[3];
 } group_run;
 
-static void *run_group(void *arg) {
-  group_run *gr = (group_run *)arg;
+#define GCK(gr, call)                                                                  \
+  do {                                                                                 \
+    int rc_ = (call);                                                                  \
+    if (rc_) {                                                                         \
+      snprintf((gr)->err, sizeof (gr)->err, "%s: %s", #call, micsa_last_error((gr)->ctx)); \
+      return rc_;                                                                      \
+    }                                                                                  \
+  } while (0)
+
+/* host buffers and the uploads of every slot (couplings, spins, streams) */
+static int group_prepare(group_run *gr) {
   const micsa_job *j0 = &gr->jobs[gr->idx[0]];
   const int nr = j0->nr, n = gr->n;
-  micsa_ctx *ctx = gr->ctx;
-  micsa_prc_t *prc = (micsa_prc_t *)malloc(sizeof(micsa_prc_t) * nr * n);
-  micsa_xoshiro_t *xo = (micsa_xoshiro_t *)malloc(sizeof(micsa_xoshiro_t) * nr * n);
-  int32_t *es = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * nr);
-  uint64_t *ed = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n * nr);
-  uint8_t *on = (uint8_t *)malloc((size_t)n);
-  int64_t *m = (int64_t *)calloc((size_t)n, sizeof(int64_t));
-  int rc = MICSA_OK;
-  if (!prc || !xo || !es || !ed || !on || !m) {
-    rc = MICSA_ERR_NOMEM;
+  gr->gprc = (micsa_prc_t *)malloc(sizeof(micsa_prc_t) * nr * n);
+  gr->gxo = (micsa_xoshiro_t *)malloc(sizeof(micsa_xoshiro_t) * nr * n);
+  gr->es = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * nr);
+  gr->ed = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n * nr);
+  gr->on = (uint8_t *)malloc((size_t)n);
+  gr->m = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+  if (!gr->gprc || !gr->gxo || !gr->es || !gr->ed || !gr->on || !gr->m) {
     snprintf(gr->err, sizeof gr->err, "host memory for a group of %d jobs", n);
-    goto out;
+    return MICSA_ERR_NOMEM;
   }
-#define CK(call)                                                                   \
-  do {                                                                             \
-    if ((rc = (call))) {                                                           \
-      snprintf(gr->err, sizeof gr->err, "%s: %s", #call, micsa_last_error(ctx));   \
-      goto out;                                                                    \
-    }                                                                              \
-  } while (0)
   for (int k = 0; k < n; k++) {
     const int j = gr->idx[k];
-    memcpy(prc + (int64_t)k * nr, gr->prc + (int64_t)j * gr->SNR, sizeof(micsa_prc_t) * nr);
-    memcpy(xo + (int64_t)k * nr, gr->xo + (int64_t)j * gr->SNR, sizeof(micsa_xoshiro_t) * nr);
-    CK(micsa_upload_couplings(ctx, k, gr->J + (int64_t)j * 12 * gr->SH));
-    CK(micsa_upload_spins(ctx, k, gr->even + (int64_t)j * gr->SH * gr->SNR,
-                          gr->odd + (int64_t)j * gr->SH * gr->SNR));
-    on[k] = 1;
+    memcpy(gr->gprc + (int64_t)k * nr, gr->prc + (int64_t)j * gr->SNR, sizeof(micsa_prc_t) * nr);
+    memcpy(gr->gxo + (int64_t)k * nr, gr->xo + (int64_t)j * gr->SNR, sizeof(micsa_xoshiro_t) * nr);
+    GCK(gr, micsa_upload_couplings(gr->ctx, k, gr->J + (int64_t)j * 12 * gr->SH));
+    GCK(gr, micsa_upload_spins(gr->ctx, k, gr->even + (int64_t)j * gr->SH * gr->SNR,
+                               gr->odd + (int64_t)j * gr->SH * gr->SNR));
+    gr->on[k] = 1;
   }
-  {
-    uint64_t thr[3];
-    micsa_thresholds(j0->beta, thr);
-    int nrun = n;
-    int64_t t = 0;
-    while (nrun > 0) {
-      /* the host advance of the streams overlaps the iterations that follow */
-      if (!(t & (t - 1))) {
-        if (!has_schedule(j0)) {
-          /* refresh t was drawn ahead (except at t = 0); draw the next one,
-           * for the jobs that run past it, while these iterations run */
-          if (t == 0)
-            CK(micsa_refresh_demons_async(ctx, 0, nrun, prc, xo, thr));
-          else
-            CK(micsa_refresh_commit(ctx));
-          const int64_t tn = t ? 2 * t : 1;
-          int nnext = 0;
-          while (nnext < nrun && gr->jobs[gr->idx[nnext]].iterations > tn) nnext++;
-          if (nnext) CK(micsa_refresh_demons_ahead(ctx, 0, nnext, prc, xo, thr));
-        } else { /* each job at its own point of its beta schedule */
-          for (int k = 0; k < nrun; k++) {
-            uint64_t tk[3];
-            micsa_thresholds(micsa_job_beta(&gr->jobs[gr->idx[k]], t), tk);
-            CK(micsa_refresh_demons_async(ctx, k, 1, prc + (int64_t)k * nr, xo + (int64_t)k * nr, tk));
-          }
-        }
-      }
-      int64_t next = 1;
-      while (next <= t) next <<= 1;
-      const int64_t last = gr->jobs[gr->idx[nrun - 1]].iterations; /* shortest running */
-      if (next > last) next = last;
-      CK(micsa_iterate(ctx, next - t));
-      t = next;
-      int any = 0;
-      for (int k = 0; k < nrun; k++) any |= is_pow2(t) || t == gr->jobs[gr->idx[k]].iterations;
-      if (!any) continue;
-      CK(micsa_measure(ctx, es, ed, NULL, NULL));
-      int still = nrun;
-      for (int k = 0; k < nrun; k++) {
-        const int j = gr->idx[k];
-        const int64_t it = gr->jobs[j].iterations;
-        if (!(is_pow2(t) || t == it)) continue;
-        const int64_t o = gr->off[j] + m[k]++ * nr;
-        if (gr->e_spin) memcpy(gr->e_spin + o, es + (int64_t)k * nr, 4 * (size_t)nr);
-        if (gr->e_demon) memcpy(gr->e_demon + o, ed + (int64_t)k * nr, 8 * (size_t)nr);
-        if (t == it) {
-          on[k] = 0;
-          still--;
-        }
-      }
-      if (still != nrun) {
-        nrun = still; /* finished jobs are the tail (longest first) */
-        CK(micsa_set_active(ctx, on));
-      }
+  micsa_thresholds(j0->beta, gr->thr);
+  gr->nrun = n;
+  return MICSA_OK;
+}
+
+/* the demon refresh of the running slots at t = 0 or a power of two */
+static int group_refresh(group_run *gr, int64_t t) {
+  if (gr->nrun < 1 || (t & (t - 1))) return MICSA_OK;
+  const micsa_job *j0 = &gr->jobs[gr->idx[0]];
+  const int nr = j0->nr;
+  micsa_ctx *ctx = gr->ctx;
+  if (!has_schedule(j0)) {
+    /* refresh t was drawn ahead (except at t = 0); draw the next one, for
+     * the jobs that run past it, while the iterations up to it run (the
+     * host advance of the streams overlaps them as well) */
+    if (t == 0)
+      GCK(gr, micsa_refresh_demons_async(ctx, 0, gr->nrun, gr->gprc, gr->gxo, gr->thr));
+    else
+      GCK(gr, micsa_refresh_commit(ctx));
+    const int64_t tn = t ? 2 * t : 1;
+    int nnext = 0;
+    while (nnext < gr->nrun && gr->jobs[gr->idx[nnext]].iterations > tn) nnext++;
+    if (nnext) GCK(gr, micsa_refresh_demons_ahead(ctx, 0, nnext, gr->gprc, gr->gxo, gr->thr));
+  } else { /* each job at its own point of its beta schedule */
+    for (int k = 0; k < gr->nrun; k++) {
+      uint64_t tk[3];
+      micsa_thresholds(micsa_job_beta(&gr->jobs[gr->idx[k]], t), tk);
+      GCK(gr, micsa_refresh_demons_async(ctx, k, 1, gr->gprc + (int64_t)k * nr,
+                                         gr->gxo + (int64_t)k * nr, tk));
     }
-    CK(micsa_refresh_wait(ctx));
-    CK(micsa_synchronize(ctx));
   }
-#undef CK
-out:
-  micsa_destroy(ctx);
+  return MICSA_OK;
+}
+
+/* the group's next event after t: a power of two or its shortest running
+ * job's end (INT64_MAX when nothing runs) */
+static int64_t group_next(const group_run *gr, int64_t t) {
+  if (gr->nrun < 1) return INT64_MAX;
+  int64_t next = 1;
+  while (next <= t) next <<= 1;
+  const int64_t last = gr->jobs[gr->idx[gr->nrun - 1]].iterations; /* shortest running */
+  return next > last ? last : next;
+}
+
+/* measurements at t of the slots that need one, and the freeze of the
+ * slots whose job ended at t */
+static int group_measure(group_run *gr, int64_t t) {
+  if (gr->nrun < 1) return MICSA_OK;
+  const int nr = gr->jobs[gr->idx[0]].nr;
+  int any = 0;
+  for (int k = 0; k < gr->nrun; k++) any |= is_pow2(t) || t == gr->jobs[gr->idx[k]].iterations;
+  if (!any) return MICSA_OK;
+  GCK(gr, micsa_measure(gr->ctx, gr->es, gr->ed, NULL, NULL));
+  int still = gr->nrun;
+  for (int k = 0; k < gr->nrun; k++) {
+    const int j = gr->idx[k];
+    const int64_t it = gr->jobs[j].iterations;
+    if (!(is_pow2(t) || t == it)) continue;
+    const int64_t o = gr->off[j] + gr->m[k]++ * nr;
+    if (gr->e_spin) memcpy(gr->e_spin + o, gr->es + (int64_t)k * nr, 4 * (size_t)nr);
+    if (gr->e_demon) memcpy(gr->e_demon + o, gr->ed + (int64_t)k * nr, 8 * (size_t)nr);
+    if (t == it) {
+      gr->on[k] = 0;
+      still--;
+    }
+  }
+  if (still != gr->nrun) {
+    gr->nrun = still; /* finished jobs are the tail (longest first) */
+    GCK(gr, micsa_set_active(gr->ctx, gr->on));
+  }
+  return MICSA_OK;
+}
+
+static int group_drain(group_run *gr) {
+  GCK(gr, micsa_refresh_wait(gr->ctx));
+  GCK(gr, micsa_synchronize(gr->ctx));
+  return MICSA_OK;
+}
+
+static void group_free(group_run *gr) {
+  micsa_destroy(gr->ctx);
   gr->ctx = NULL;
-  free(prc), free(xo), free(es), free(ed), free(on), free(m);
+  free(gr->gprc), free(gr->gxo), free(gr->es), free(gr->ed), free(gr->on), free(gr->m);
+  gr->gprc = NULL, gr->gxo = NULL, gr->es = NULL, gr->ed = NULL, gr->on = NULL, gr->m = NULL;
+}
+#undef GCK
+
+/* a group on its own host thread and stream */
+static void *run_group(void *arg) {
+  group_run *gr = (group_run *)arg;
+  int rc = group_prepare(gr);
+  for (int64_t t = 0; !rc && gr->nrun > 0;) {
+    if ((rc = group_refresh(gr, t))) break;
+    const int64_t next = group_next(gr, t);
+    if ((rc = micsa_iterate(gr->ctx, next - t))) {
+      snprintf(gr->err, sizeof gr->err, "micsa_iterate: %s", micsa_last_error(gr->ctx));
+      break;
+    }
+    t = next;
+    rc = group_measure(gr, t);
+  }
+  if (!rc) rc = group_drain(gr);
+  group_free(gr);
   gr->rc = rc;
   return NULL;
+}
+
+/* All groups in lockstep on one host thread: every group's refreshes and
+ * measurements at the common event times, and the iterations between them
+ * as mixed-lattice launches (one per iteration for all groups of one
+ * replica count).  Each job's numbers are the same as in run_group. */
+static int run_lockstep(group_run *grs, int ng, char *err, size_t errlen) {
+  int rc = MICSA_OK;
+  micsa_multi *multi[8] = {0};
+  int nm = 0;
+  /* one mixed launch per replica count, up to 16 groups each; created
+   * before any upload, so that its launch shape is timed on empty buffers */
+  {
+    int used[64] = {0};
+    if (ng > 64) {
+      rc = MICSA_ERR_UNSUPPORTED;
+      errf(err, errlen, "lockstep batches take at most 64 shape groups, got %d", ng);
+      goto out;
+    }
+    for (int a = 0; a < ng; a++) {
+      if (used[a]) continue;
+      micsa_ctx *cs[16];
+      int k = 0;
+      for (int b = a; b < ng && k < 16; b++)
+        if (!used[b] && grs[b].jobs[grs[b].idx[0]].nr == grs[a].jobs[grs[a].idx[0]].nr) {
+          used[b] = 1;
+          cs[k++] = grs[b].ctx;
+        }
+      if (nm == 8) {
+        rc = MICSA_ERR_UNSUPPORTED;
+        errf(err, errlen, "too many mixed launches");
+        goto out;
+      }
+      if ((rc = micsa_multi_create(cs, k, &multi[nm], err, errlen))) goto out;
+      nm++;
+    }
+  }
+  for (int g = 0; g < ng && !rc; g++) rc = group_prepare(&grs[g]);
+  if (rc) goto group_err;
+  {
+    int64_t t = 0;
+    for (;;) {
+      int64_t next = INT64_MAX;
+      for (int g = 0; g < ng; g++) {
+        if ((rc = group_refresh(&grs[g], t))) goto group_err;
+        const int64_t n = group_next(&grs[g], t);
+        if (n < next) next = n;
+      }
+      if (next == INT64_MAX) break;
+      for (int k = 0; k < nm; k++)
+        if ((rc = micsa_multi_iterate(multi[k], next - t))) {
+          errf(err, errlen, "micsa_multi_iterate: %s", micsa_multi_last_error(multi[k]));
+          goto out;
+        }
+      t = next;
+      for (int g = 0; g < ng; g++)
+        if ((rc = group_measure(&grs[g], t))) goto group_err;
+    }
+    for (int k = 0; k < nm; k++)
+      if ((rc = micsa_multi_synchronize(multi[k]))) {
+        errf(err, errlen, "micsa_multi_synchronize: %s", micsa_multi_last_error(multi[k]));
+        goto out;
+      }
+    for (int g = 0; g < ng; g++)
+      if ((rc = group_drain(&grs[g]))) goto group_err;
+  }
+  goto out;
+group_err:
+  for (int g = 0; g < ng; g++)
+    if (grs[g].err[0]) {
+      errf(err, errlen, "%s", grs[g].err);
+      break;
+    }
+out:
+  for (int k = 0; k < nm; k++) micsa_multi_destroy(multi[k]);
+  for (int g = 0; g < ng; g++) group_free(&grs[g]);
+  return rc;
+}
+
+/* MICSA_BATCH=multi: every shape group in lockstep through the
+ * mixed-lattice launch; groups: each group on its own stream and host
+ * thread (the default) */
+static int batch_lockstep(void) {
+  const char *e = getenv("MICSA_BATCH");
+  return e && !strcmp(e, "multi");
 }
 
 static int same_group(const micsa_job *a, const micsa_job *b) {
@@ -328,18 +462,33 @@ int micsa_run_batch(int device, const micsa_job *jobs, int njobs, int32_t *e_spi
         snprintf(grs[g].err, sizeof grs[g].err, "micsa_create L=%d nr=%d n=%d failed (%d)", j0->L,
                  j0->nr, grs[g].n, grs[g].rc);
     }
-    for (int g = 0; g < ng; g++) {
-      if (!grs[g].ctx) continue;
-      spawned[g] = g < ng - 1 && pthread_create(&tid[g], NULL, run_group, &grs[g]) == 0;
-      if (!spawned[g]) run_group(&grs[g]);
-    }
-    for (int g = 0; g < ng; g++) {
-      if (spawned[g]) pthread_join(tid[g], NULL);
-      if (grs[g].rc && !rc) {
-        rc = grs[g].rc;
-        errf(err, errlen, "%s", grs[g].err);
+    int created = 1;
+    for (int g = 0; g < ng; g++)
+      if (!grs[g].ctx) {
+        created = 0;
+        if (!rc) {
+          rc = grs[g].rc;
+          errf(err, errlen, "%s", grs[g].err);
+        }
+      }
+    if (created && batch_lockstep()) {
+      rc = run_lockstep(grs, ng, err, errlen);
+    } else {
+      for (int g = 0; g < ng; g++) {
+        if (!grs[g].ctx) continue;
+        spawned[g] = g < ng - 1 && pthread_create(&tid[g], NULL, run_group, &grs[g]) == 0;
+        if (!spawned[g]) run_group(&grs[g]);
+      }
+      for (int g = 0; g < ng; g++) {
+        if (spawned[g]) pthread_join(tid[g], NULL);
+        if (grs[g].rc && !rc) {
+          rc = grs[g].rc;
+          errf(err, errlen, "%s", grs[g].err);
+        }
       }
     }
+    for (int g = 0; g < ng; g++)
+      if (grs[g].ctx) group_free(&grs[g]); /* groups that never ran */
     if (seconds) *seconds = now_s() - t0;
   }
 done:

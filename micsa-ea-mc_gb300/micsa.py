@@ -32,7 +32,9 @@ ABI_SYMBOLS = [
     "micsa_synchronize", "micsa_kernel_launches", "micsa_stream", "micsa_job_measurements",
     "micsa_run_batch", "micsa_set_active", "micsa_serve", "micsa_job_beta",
     "micsa_server_create", "micsa_submit", "micsa_poll", "micsa_server_destroy",
-    "micsa_debug_flow_waits",
+    "micsa_debug_flow_waits", "micsa_multi_create", "micsa_multi_iterate",
+    "micsa_multi_synchronize", "micsa_multi_destroy", "micsa_multi_last_error",
+    "micsa_multi_kernel_launches", "micsa_multi_report",
 ]
 NOALLOC_MAX_REPLICAS = 8192
 NOALLOC_MAX_L = 888
@@ -156,6 +158,14 @@ def lib():
         "micsa_job_measurements": (C.c_int64, [C.c_int64]),
         "micsa_set_active": (C.c_int, [C.c_void_p, u8p]),
         "micsa_debug_flow_waits": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int]),
+        "micsa_multi_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p),
+                                         C.c_char_p, C.c_size_t]),
+        "micsa_multi_iterate": (C.c_int, [C.c_void_p, C.c_int64]),
+        "micsa_multi_synchronize": (C.c_int, [C.c_void_p]),
+        "micsa_multi_destroy": (C.c_int, [C.c_void_p]),
+        "micsa_multi_last_error": (C.c_char_p, [C.c_void_p]),
+        "micsa_multi_kernel_launches": (C.c_int64, [C.c_void_p]),
+        "micsa_multi_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
         "micsa_job_beta": (C.c_double, [C.POINTER(Job), C.c_int64]),
         "micsa_serve": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(Request), C.c_int,
                                   C.POINTER(RequestResult), i32p, u64p, C.POINTER(C.c_double),
@@ -378,6 +388,56 @@ class Context:
 
 
 # ------------------------------------------------------------------ host side
+class Multi:
+    """Mixed-lattice launches over several contexts (micsa_multi_*)."""
+
+    def __init__(self, contexts):
+        self.contexts = list(contexts)
+        arr = (C.c_void_p * len(self.contexts))(*[c.h for c in self.contexts])
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        rc = lib().micsa_multi_create(arr, len(self.contexts), C.byref(h), err, 512)
+        if rc != MICSA_OK:
+            raise MicsaError("micsa_multi_create failed (%d): %s" % (rc, err.value.decode()))
+        self.h = h
+
+    def _check(self, rc, what):
+        if rc != MICSA_OK:
+            raise MicsaError("%s failed (%d): %s" % (what, rc,
+                                                    lib().micsa_multi_last_error(self.h).decode()))
+
+    def iterate(self, n):
+        self._check(lib().micsa_multi_iterate(self.h, n), "micsa_multi_iterate")
+
+    def synchronize(self):
+        self._check(lib().micsa_multi_synchronize(self.h), "micsa_multi_synchronize")
+
+    def report(self):
+        b = C.create_string_buffer(8192)
+        lib().micsa_multi_report(self.h, b, 8192)
+        return b.value.decode()
+
+    def kernel_launches(self):
+        return lib().micsa_multi_kernel_launches(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().micsa_multi_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Streams:
     """Host generator state of one run (the reference's globals of ini.c)."""
 

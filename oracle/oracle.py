@@ -52,6 +52,97 @@ def build_reference(L, nr, ms=2):
     return exe
 
 
+REF_GPU_LIB = os.path.join(LIBDIR, "libref_gpu.so")
+
+
+def build_ref_gpu_harness(force=False):
+    """The host side that drives the reference's own CUDA kernels
+    (ref_gpu/ref_gpu_harness.cu; our code, test infrastructure)."""
+    src = os.path.join(HERE, "ref_gpu", "ref_gpu_harness.cu")
+    os.makedirs(LIBDIR, exist_ok=True)
+    if not force and os.path.exists(REF_GPU_LIB) and os.path.getmtime(REF_GPU_LIB) >= os.path.getmtime(src):
+        return REF_GPU_LIB
+    nvcc = "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc"
+    stubs = "/usr/local/cuda/lib64/stubs"
+    subprocess.run([nvcc, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", src, "-o", REF_GPU_LIB,
+                    "-L" + stubs, "-lcuda"], check=True, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    return REF_GPU_LIB
+
+
+def ref_gpu_cubin(L, nr, ms=2, build=False):
+    """The reference's device code for (L, NR, MAXNSAMPLES) compiled for
+    sm_103a (ref_gpu/build_ref_gpu.sh); built only where the reference
+    sources are present, else whatever was built there before."""
+    path = os.path.join(REF_DIR, "micsa_ref_gpu_L%d_NR%d_MS%d.cubin" % (L, nr, ms))
+    if os.path.exists(path) or not build or not reference_available():
+        return path if os.path.exists(path) else None
+    subprocess.run(["sh", os.path.join(HERE, "ref_gpu", "build_ref_gpu.sh"), str(L), str(nr), str(ms)],
+                   check=True, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    return path
+
+
+class RefGPU:
+    """The reference's CUDA kernels for ns samples of one (L, nr) build, on
+    device 0, laid out and launched as the reference's main.cu does."""
+
+    def __init__(self, cubin, L, nr, ns, nc):
+        self.lib = C.CDLL(build_ref_gpu_harness())
+        self.lib.rg_error.restype = C.c_char_p
+        self.L, self.nr, self.ns, self.nc = L, nr, ns, nc
+        neig, rot = tables(L)
+        neig = np.ascontiguousarray(neig.reshape(-1))
+        rot = np.ascontiguousarray(rot.reshape(-1))
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        rc = self.lib.rg_create(cubin.encode(), L, nr, ns, nc, _p(neig, I32), _p(rot, U8), C.byref(h),
+                                err, 512)
+        if rc:
+            raise RuntimeError("reference kernels: %s" % err.value.decode())
+        self.h = h
+
+    def _ck(self, rc, what):
+        if rc:
+            raise RuntimeError("%s: %s" % (what, self.lib.rg_error(self.h).decode()))
+
+    def upload(self, s, J, even, odd, w0, w1):
+        self._ck(self.lib.rg_upload(self.h, s, None if J is None else _p(J, U64), _p(even, U64),
+                                    _p(odd, U64), _p(w0, U64), _p(w1, U64)), "rg_upload")
+
+    def download(self, s):
+        H = (self.L // 4) ** 3 // 2
+        e = np.zeros(H * self.nr, np.uint64)
+        o = np.zeros(H * self.nr, np.uint64)
+        w0 = np.zeros(2 * H * self.nc * self.nr, np.uint64)
+        w1 = np.zeros(2 * H * self.nc * self.nr, np.uint64)
+        self._ck(self.lib.rg_download(self.h, s, _p(e, U64), _p(o, U64), _p(w0, U64), _p(w1, U64)),
+                 "rg_download")
+        return e, o, w0, w1
+
+    def iterate(self, n):
+        self._ck(self.lib.rg_iterate(self.h, C.c_int64(n)), "rg_iterate")
+
+    def time(self, warm, n):
+        ms = C.c_double()
+        self._ck(self.lib.rg_time(self.h, C.c_int64(warm), C.c_int64(n), C.byref(ms)), "rg_time")
+        return ms.value
+
+    def launch_shape(self):
+        a, b = C.c_int(), C.c_int()
+        self.lib.rg_launch_shape(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def lib():
     global _lib
     if _lib is None:

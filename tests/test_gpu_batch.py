@@ -14,6 +14,14 @@ pytestmark = pytest.mark.gpu
 BETA = 0.9090909090909
 
 
+@pytest.fixture(params=["groups", "multi"])
+def batch_mode(request, monkeypatch):
+    """groups: each shape group on its own stream and host thread; multi:
+    all groups in lockstep, their iterations as mixed-lattice launches."""
+    monkeypatch.setenv("MICSA_BATCH", request.param)
+    return request.param
+
+
 def _jobs(n, L, nr, nc, iters, base):
     return [dict(L=L, nr=nr, nc=nc, iterations=iters, seed_J=base + 101 * j + 1,
                  seed_u=base + 7 * j + 3, beta=BETA) for j in range(n)]
@@ -54,7 +62,7 @@ def _oracle_job(job):
     return np.array(out_s), np.array(out_d)
 
 
-def test_batch_job_equals_oracle_on_reference_schedule():
+def test_batch_job_equals_oracle_on_reference_schedule(batch_mode):
     jobs = _jobs(3, 8, 32, 6, 21, 77)
     es, ed, _ = micsa.run_batch(jobs)
     for j in range(3):
@@ -63,14 +71,17 @@ def test_batch_job_equals_oracle_on_reference_schedule():
         assert np.array_equal(ed[j], od.astype(np.uint64)), j
 
 
-def test_batch_mixed_shapes_and_lengths_equal_alone():
+def test_batch_mixed_shapes_and_lengths_equal_alone(batch_mode, monkeypatch):
     """Uneven L, replica counts and iteration counts in one call: shape
-    groups run concurrently, jobs finish at their own lengths."""
+    groups run concurrently (or in lockstep through the mixed-lattice
+    launch), jobs finish at their own lengths; each job equals the job run
+    alone in the other mode as well."""
     shapes = [(8, 32, 37), (16, 64, 64), (24, 32, 20), (8, 32, 5), (16, 64, 9), (24, 32, 64),
               (8, 32, 64), (40, 32, 3)]
     jobs = [dict(L=L, nr=nr, nc=4, iterations=it, seed_J=900 + 17 * k, seed_u=55 + 3 * k, beta=BETA)
             for k, (L, nr, it) in enumerate(shapes)]
     es, ed, _ = micsa.run_batch(jobs)
+    monkeypatch.setenv("MICSA_BATCH", "groups" if batch_mode == "multi" else "multi")
     for j, job in enumerate(jobs):
         e1, d1, _ = micsa.run_batch([job])
         assert es[j].shape == (micsa.lib().micsa_job_measurements(job["iterations"]), job["nr"])
@@ -95,7 +106,7 @@ def test_batch_512_samples_headline_batched_shape():
         assert np.array_equal(es[j], e1[0]) and np.array_equal(ed[j], d1[0]), j
 
 
-def test_batch_beta_schedule_equals_alone_and_oracle():
+def test_batch_beta_schedule_equals_alone_and_oracle(batch_mode):
     """Linear beta schedule (an extension: the reference has one beta): each
     refresh draws the demons at beta(t); the batch equals the jobs alone and
     the oracle with the thresholds recomputed at every refresh."""
