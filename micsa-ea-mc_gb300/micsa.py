@@ -149,9 +149,9 @@ def lib():
         "micsa_profile": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double),
                                     C.POINTER(C.c_double)]),
         "micsa_tuning_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+        # (L, nr, nsamples, spin_rows, J_rows, e_spin, stream, err, errlen)
         "micsa_energy_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
-                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
-                                           C.c_size_t]),
+                                           C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]),
         "micsa_synchronize": (C.c_int, [C.c_void_p]),
         "micsa_kernel_launches": (C.c_int64, [C.c_void_p]),
         "micsa_stream": (C.c_void_p, [C.c_void_p]),

@@ -227,3 +227,20 @@ def test_every_environment_variable_is_documented():
     assert lib_names and drv_names
     assert not [n for n in sorted(lib_names) if n not in header]
     assert not [n for n in sorted(drv_names) if n not in usage]
+
+
+def test_noalloc_entry_point_checks_its_arguments_before_any_device_work():
+    """micsa_energy_noalloc rejects impossible sizes and missing row tables
+    before it touches a device, so these calls need no GPU; they also check
+    that the binding's argument list matches the declaration."""
+    err = C.create_string_buffer(256)
+    f = micsa.lib().micsa_energy_noalloc
+    dummy = (C.c_void_p * 64)(*([16] * 64))
+    assert f(16, micsa.NOALLOC_MAX_REPLICAS, 2, dummy, dummy, C.c_void_p(16), None, err, 256) == 1
+    assert b"exceeds" in err.value
+    assert f(micsa.NOALLOC_MAX_L + 8, 32, 1, dummy, dummy, C.c_void_p(16), None, err, 256) == 1
+    assert b"888" in err.value
+    assert f(16, 32, 1, None, dummy, C.c_void_p(16), None, err, 256) == 1
+    nulls = (C.c_void_p * 24)()
+    assert f(16, 32, 1, dummy, nulls, C.c_void_p(16), None, err, 256) == 1
+    assert b"coupling row 0" in err.value
