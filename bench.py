@@ -261,8 +261,11 @@ def run_micsa(a, dist):
     peak, kind = peaks()
     traffic, tnote = traffic_per_launch(L, nr, ns, "k_sweep_dep" if "load=flow" in ctx.tuning()
                                         else "k_sweep")
-    kernel = ("k_sweep_dep (dataflow sweep: the %d half-sweeps of an iteration in one launch; "
-              "time per half-sweep)" % (2 * nc) if "load=flow" in ctx.tuning()
+    fit = 1
+    if "fit=" in ctx.tuning():
+        fit = int(ctx.tuning().split("fit=")[1].split()[0].rstrip("|"))
+    kernel = ("k_sweep_dep (dataflow sweep: the %d half-sweeps of each of %d iteration(s) in one "
+              "launch; time per half-sweep)" % (2 * nc, fit) if "load=flow" in ctx.tuning()
               else "k_sweep (micSA half-sweep)")
     roof = {"bound": "hbm", "kernel": kernel,
             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

@@ -32,6 +32,7 @@
  *   MICSA_PDL=0          plain launches instead of programmatic dependent launch
  *   MICSA_REFRESH_WPS=n  segment length of the GPU demon refresh, in words
  *   MICSA_REFRESH_OCC=1  the refresh kernel without its register budget
+ *   MICSA_FLOW_ITERS=k   iterations per dataflow launch, with a pinned shape
  *   MICSA_SWEEP_PF=n     the dataflow sweep requests n demon planes of each tile
  *                        into L2 before its dependency wait
  *   MICSA_MULTI_ZC=z     slab depth of the mixed-lattice launch (no timing)
@@ -187,7 +188,9 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
  * tile, ordered by per-slab dependency counters; split then orders its
  * tiles sample-major (1) or half-sweep-major (0) | quad: direct loads with
  * four one-word sites per thread (32 replicas)>
- * tile=<default | row: blocks span whole rows along x> |
+ * tile=<default | row: blocks span whole rows along x>
+ * fit=<iterations per launch of the dataflow sweep: its wavefront runs on
+ * from one iteration into the next; 1 for the other loads> |
  * <zc>/<pd>/<split>/<occ>/<load 0|1|2|3|4|5>/<tile 0|1>:<ms per half-sweep> ...",
  * with " cached" before the "|" when the choice and its table were taken
  * over from an earlier context of the same device, L, nr, samples and nc in

@@ -43,7 +43,10 @@ struct micsa_ctx {
   std::vector<int> have_j, have_spin, have_dem;
   std::vector<uint8_t> active_host; /* host copy of the run flags */
   cudaGraph_t graph = nullptr;
-  cudaGraphExec_t graph_exec = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;   /* g.fit iterations (dataflow), else one */
+  cudaGraph_t graph1 = nullptr;
+  cudaGraphExec_t graph1_exec = nullptr;  /* one iteration, when g.fit > 1 */
+  int64_t graph1_launches = 0;
   int64_t launches = 0;
   int resident = 0;        /* small lattice: iterations run in shared memory */
   int split = 0;           /* k > 0: half-sweep launches per group of k samples, group-major
@@ -234,7 +237,7 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
  * choice and table instead of timing again, so batches and servers that open
  * many contexts of a few shapes pay for each shape once. */
 struct tune_entry {
-  int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, n;
+  int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, fit, n;
   std::vector<int> zcs, pds, splits, occs, loads, tws;
   std::vector<double> ms;
 };
@@ -284,6 +287,10 @@ int autotune(micsa_ctx *ctx) {
     g.tw = ew && !strcmp(ew, "row") && !g.tma && micsa_sweep_wide_differs(g.L, eq && atoi(eq) ? 4 : 2);
     g.flow = ef && atoi(ef) && !g.tma && !g.async && !g.pipe;
     g.quad = eq && atoi(eq) && g.W == 1 && !g.tma && !g.async && !g.pipe && !g.flow;
+    if (const char *ek = getenv("MICSA_FLOW_ITERS")) {
+      const int k = atoi(ek);
+      if (g.flow && k >= 1 && k <= 64) g.fit = k;
+    }
     const int oc = eo ? atoi(eo) : 3;
     g.occ = g.pipe ? (oc == 2 ? 2 : 3) : (oc == 4 ? 4 : 3);
     ctx->ntune = 0;
@@ -306,6 +313,7 @@ int autotune(micsa_ctx *ctx) {
       g.tw = t.tw;
       g.flow = t.flow;
       g.quad = t.quad;
+      g.fit = t.fit;
       ctx->ntune = t.n;
       for (int c = 0; c < t.n; c++) {
         ctx->tune_zc[c] = t.zcs[c];
@@ -430,6 +438,41 @@ int autotune(micsa_ctx *ctx) {
   g.tw = best_tw;
   g.flow = best_flow;
   g.quad = best_quad;
+  g.fit = 1;
+  if (g.flow) {
+    /* iterations per dataflow launch: the wavefront runs on from one
+     * iteration into the next instead of draining the GPU at every launch
+     * boundary; timed per iteration on graphs of k iterations */
+    double best_it = 1e30;
+    int best_fit = 1;
+    for (int k : {1, 4, 16}) {
+      g.fit = k;
+      cudaGraph_t gr = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t le = launch_halves(ctx, g, ctx->split, 0, g.nc, nullptr);
+      if (le == cudaSuccess) le = micsa_launch_walk_add(g, ctx->walk, k, ctx->stream);
+      const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &gr);
+      MICSA_CK(le);
+      MICSA_CK(ce);
+      const cudaError_t ie = cudaGraphInstantiate(&ge, gr, 0);
+      cudaGraphDestroy(gr);
+      MICSA_CK(ie);
+      const int r = k >= 16 ? 1 : (k >= 4 ? 2 : 6);
+      float ms = 0;
+      cudaError_t te = cudaGraphLaunch(ge, ctx->stream);
+      if (te == cudaSuccess) te = cudaEventRecord(e0, ctx->stream);
+      for (int rep = 0; rep < r && te == cudaSuccess; rep++) te = cudaGraphLaunch(ge, ctx->stream);
+      if (te == cudaSuccess) te = cudaEventRecord(e1, ctx->stream);
+      if (te == cudaSuccess) te = cudaEventSynchronize(e1);
+      if (te == cudaSuccess) te = cudaEventElapsedTime(&ms, e0, e1);
+      cudaGraphExecDestroy(ge);
+      MICSA_CK(te);
+      const double per = ms / ((double)r * k);
+      if (per < best_it) best_it = per, best_fit = k;
+    }
+    g.fit = best_fit;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (use_cache) {
@@ -444,6 +487,7 @@ int autotune(micsa_ctx *ctx) {
     t.tw = g.tw;
     t.flow = g.flow;
     t.quad = g.quad;
+    t.fit = g.fit;
     t.n = n;
     t.zcs.assign(ctx->tune_zc, ctx->tune_zc + n);
     t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
@@ -458,12 +502,40 @@ int autotune(micsa_ctx *ctx) {
   return MICSA_OK;
 }
 
-/* one iteration's launches; *launches counts them */
-int enqueue_micsa_iteration(micsa_ctx *ctx, int64_t *launches) {
-  const micsa_geo &g = ctx->g;
+/* the launches of k iterations (k > 1 only with the dataflow sweep, which
+ * carries them in one launch); *launches counts them */
+int enqueue_micsa_iterations(micsa_ctx *ctx, int k, int64_t *launches) {
+  micsa_geo g = ctx->g;
+  g.fit = g.flow ? k : 1;
+  if (!g.flow && k != 1) return fail(ctx, MICSA_ERR_STATE, "several iterations per launch");
   MICSA_CK(launch_halves(ctx, g, ctx->split, 0, g.nc, launches));
-  MICSA_CK(micsa_launch_walk_advance(g, ctx->walk, ctx->stream));
+  if (k == 1)
+    MICSA_CK(micsa_launch_walk_advance(g, ctx->walk, ctx->stream));
+  else
+    MICSA_CK(micsa_launch_walk_add(g, ctx->walk, k, ctx->stream));
   if (launches) ++*launches;
+  return MICSA_OK;
+}
+
+int enqueue_micsa_iteration(micsa_ctx *ctx, int64_t *launches) {
+  return enqueue_micsa_iterations(ctx, 1, launches);
+}
+
+/* the iteration graph of k iterations */
+int capture_iterations(micsa_ctx *ctx, int k, cudaGraph_t *graph, cudaGraphExec_t *exec,
+                       int64_t *launches) {
+  MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  *launches = 0;
+  int rc = enqueue_micsa_iterations(ctx, k, launches);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  MICSA_CK(e);
+  *graph = g;
+  MICSA_CK(cudaGraphInstantiate(exec, g, 0));
   return MICSA_OK;
 }
 
@@ -509,6 +581,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.tw = 0;
   g.flow = 0;
   g.quad = 0;
+  g.fit = 1;
   {
     /* MICSA_SWEEP_PF=n: the dataflow sweep requests n demon planes of each
      * tile into L2 before its dependency wait (0: none) */
@@ -596,10 +669,11 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s%s |", ctx->g.zc,
+  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s fit=%d%s |", ctx->g.zc,
                    ctx->g.pd, ctx->split, ctx->g.occ,
                    ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : (ctx->g.flow ? "flow" : (ctx->g.quad ? "quad" : "direct")))),
-                   ctx->g.tw ? "row" : "default", ctx->tune_cached ? " cached" : "");
+                   ctx->g.tw ? "row" : "default", ctx->g.flow ? ctx->g.fit : 1,
+                   ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
     k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],
                   ctx->tune_pd[c], ctx->tune_split[c], ctx->tune_occ[c], ctx->tune_load[c],
@@ -623,6 +697,8 @@ int micsa_destroy(micsa_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  if (ctx->graph1_exec) cudaGraphExecDestroy(ctx->graph1_exec);
+  if (ctx->graph1) cudaGraphDestroy(ctx->graph1);
   void *bufs[] = {ctx->spin, ctx->dem0,     ctx->dem1,    ctx->rnd,      ctx->jb,
                   ctx->lut,  ctx->te,       ctx->keys,    ctx->walk,     ctx->stage,
                   ctx->acc,  ctx->plan_lcg, ctx->plan_xo, ctx->plan_fib, ctx->rec,
@@ -971,20 +1047,15 @@ int micsa_iterate(micsa_ctx *ctx, int64_t n) {
   if (!ctx || n < 0) return fail(ctx, MICSA_ERR_ARG, "bad argument");
   int rc = set_device(ctx);
   if (rc || (rc = ready_for_sweeps(ctx, 1))) return rc;
-  if (!ctx->graph_exec && !ctx->resident) {
-    MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    ctx->graph_launches = 0;
-    rc = enqueue_micsa_iteration(ctx, &ctx->graph_launches);
-    cudaGraph_t graph = nullptr;
-    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
-    if (rc) {
-      if (graph) cudaGraphDestroy(graph);
-      return rc;
-    }
-    MICSA_CK(e);
-    ctx->graph = graph;
-    MICSA_CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
-  }
+  /* the graph replays ctx->g.fit iterations at a time (the dataflow sweep may
+   * carry several per launch); a one-iteration graph takes the remainder */
+  const int unit = ctx->g.flow && ctx->g.fit > 1 ? ctx->g.fit : 1;
+  if (!ctx->graph_exec && !ctx->resident &&
+      (rc = capture_iterations(ctx, unit, &ctx->graph, &ctx->graph_exec, &ctx->graph_launches)))
+    return rc;
+  if (unit > 1 && n % unit && !ctx->graph1_exec &&
+      (rc = capture_iterations(ctx, 1, &ctx->graph1, &ctx->graph1_exec, &ctx->graph1_launches)))
+    return rc;
   if (ctx->resident) {
     /* small lattices: whole iterations in shared memory, up to 1024 per launch */
     for (int64_t done = 0; done < n;) {
@@ -996,8 +1067,13 @@ int micsa_iterate(micsa_ctx *ctx, int64_t n) {
     }
     return MICSA_OK;
   }
-  for (int64_t i = 0; i < n; i++) MICSA_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
-  ctx->launches += n * ctx->graph_launches;
+  for (int64_t i = 0; i < n / unit; i++) MICSA_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+  ctx->launches += n / unit * ctx->graph_launches;
+  if (unit > 1)
+    for (int64_t i = 0; i < n % unit; i++) {
+      MICSA_CK(cudaGraphLaunch(ctx->graph1_exec, ctx->stream));
+      ctx->launches += ctx->graph1_launches;
+    }
   return MICSA_OK;
 }
 
@@ -1083,10 +1159,12 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
   int rc = set_device(ctx);
   if (rc || (rc = ready_for_sweeps(ctx, 1))) return rc;
   const micsa_geo &g = ctx->g;
-  const int per = 2 * g.nc;
-  /* one iteration as a CUDA graph, as micsa_iterate runs it, with event
-   * nodes before the half-sweeps, between them and the walk, and after it;
-   * each replay is read back before the next */
+  const int unit = g.flow && g.fit > 1 ? g.fit : 1;
+  const int per = 2 * g.nc * unit;
+  /* one launch unit (g.fit iterations of the dataflow sweep, else one) as a
+   * CUDA graph, as micsa_iterate runs it, with event nodes before the
+   * half-sweeps, between them and the walk, and after it; each replay is
+   * read back before the next */
   cudaEvent_t ev[3];
   for (auto &e : ev) MICSA_CK(cudaEventCreate(&e));
   cudaGraph_t graph = nullptr;
@@ -1098,7 +1176,9 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
     e = cudaEventRecordWithFlags(ev[0], ctx->stream, cudaEventRecordExternal);
     if (e == cudaSuccess) e = launch_halves(ctx, g, ctx->split, 0, g.nc, &nl);
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[1], ctx->stream, cudaEventRecordExternal);
-    if (e == cudaSuccess) e = micsa_launch_walk_advance(g, ctx->walk, ctx->stream);
+    if (e == cudaSuccess)
+      e = unit > 1 ? micsa_launch_walk_add(g, ctx->walk, unit, ctx->stream)
+                   : micsa_launch_walk_advance(g, ctx->walk, ctx->stream);
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal);
     const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
     if (e == cudaSuccess) e = e2;
@@ -1119,7 +1199,7 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
   for (auto &x : ev) cudaEventDestroy(x);
   MICSA_CK(e);
   if (sweep_ms) *sweep_ms = sweep / (double)(n * per);
-  if (iteration_ms) *iteration_ms = total / (double)n;
+  if (iteration_ms) *iteration_ms = total / (double)(n * unit);
   return MICSA_OK;
 }
 

@@ -845,7 +845,7 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
     cst[C_T] = T;
     cst[C_YT] = (unsigned)ytiles;
     cst[C_PER_HALF] = nslab * T;
-    cst[C_PER_SAMPLE] = 2u * (unsigned)g.nc * nslab * T;
+    cst[C_PER_SAMPLE] = (unsigned)(g.fit > 1 ? g.fit : 1) * 2u * (unsigned)g.nc * nslab * T;
     cst[C_SMAJ] = (unsigned)smaj;
     dep_take(g, walk, ctl, cst, job);
   }
@@ -853,19 +853,23 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
   /* the tile's demon words are independent of the half-sweep before it:
    * on their way into L2 while the lead thread waits for the dependencies
    * (at most pf planes: the z loop's own prefetch takes over from there) */
+  /* half-sweep J of the launch is half-sweep J % 2nc of its iteration J / 2nc,
+   * whose demons sit one walk step further per iteration */
+  const unsigned per_it = 2u * (unsigned)g.nc, J = job[1];
+  const unsigned jj = J % per_it;
+  const int kwalk = (int)((job[6] + J / per_it) % (unsigned)g.Lh);
   if (pf > 0 && !micsa_frozen(g, (int)job[0]))
-    prefetch_tile_demons<VW>(g, (int)(job[1] & 1u), (int)(job[1] >> 1), job[0], job[5], job[4],
-                             job[3], job[2] * (unsigned)zc, pf < zc ? pf : zc, (int)job[6], d0,
-                             d1);
+    prefetch_tile_demons<VW>(g, (int)(jj & 1u), (int)(jj >> 1), job[0], job[5], job[4], job[3],
+                             job[2] * (unsigned)zc, pf < zc ? pf : zc, kwalk, d0, d1);
   if (lead) dep_wait(g, ctl, cst, job);
   __syncthreads();
   {
-    const unsigned s = job[0], j = job[1];
+    const unsigned s = job[0];
     if (!micsa_frozen(g, (int)s)) {
       micsa_tma none;
-      sweep_block<VW, true, WIDE, false, true>(g, (int)(j & 1u), (int)(j >> 1), s, job[5], job[4],
-                                               job[3], job[2] * (unsigned)zc, zc, pd, (int)job[6],
-                                               spin, d0, d1, jb, nullptr, none);
+      sweep_block<VW, true, WIDE, false, true>(g, (int)(jj & 1u), (int)(jj >> 1), s, job[5],
+                                               job[4], job[3], job[2] * (unsigned)zc, zc, pd,
+                                               kwalk, spin, d0, d1, jb, nullptr, none);
     }
   }
   __syncthreads();
@@ -1914,7 +1918,8 @@ static cudaError_t sweep_flow_vw(const micsa_geo &g, int smaj, uint32_t *spin, u
   const int ytiles = (g.L + ty - 1) / ty;
   const int zc = g.zc > 0 ? g.zc : 4;
   if (g.L % zc) return cudaErrorInvalidValue;
-  const int64_t tiles = (int64_t)g.ns * 2 * g.nc * (g.L / zc) * (g.Lh / 2 / tx) * ytiles * G;
+  const int64_t tiles = (int64_t)(g.fit > 1 ? g.fit : 1) * g.ns * 2 * g.nc * (g.L / zc) *
+                        (g.Lh / 2 / tx) * ytiles * G;
   if (tiles >= (1LL << 31)) return cudaErrorInvalidValue; /* 32-bit tickets */
   const dim3 block(tx, ty);
   constexpr int B0 = VW == 4 ? 2 : 3, B1 = VW == 4 ? 2 : 4;
@@ -2351,6 +2356,11 @@ k_resident(const micsa_geo g, const int n, uint32_t *__restrict__ spin,
 __global__ void k_walk_add(const micsa_geo g, int *walk, int ns, int n, int period) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < ns && !micsa_frozen(g, s)) walk[s] = (int)(((int64_t)walk[s] + n) % period);
+}
+
+cudaError_t micsa_launch_walk_add(const micsa_geo &g, int *walk, int n, cudaStream_t st) {
+  k_walk_add<<<(g.ns + 127) / 128, 128, 0, st>>>(g, walk, g.ns, n, g.L / 2);
+  return cudaGetLastError();
 }
 
 size_t micsa_resident_smem(int L, int nc) {

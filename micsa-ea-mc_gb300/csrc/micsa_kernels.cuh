@@ -39,6 +39,7 @@ struct micsa_geo {
   int quad;   /* 1: four one-word sites per sweep thread (W = 1, direct loads) */
   int pf;     /* dataflow sweep: demon planes of its tile requested into L2 before its
                  dependency wait (0 = none) */
+  int fit;    /* dataflow sweep: iterations carried by one launch (>= 1) */
   int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */
@@ -79,10 +80,11 @@ cudaError_t micsa_launch_sweep_micsa(const micsa_geo &g, int p, int ic,
                                      uint32_t *spin, uint32_t *d0, uint32_t *d1,
                                      const uint8_t *jb, const int *walk,
                                      const micsa_tma *tm, cudaStream_t st);
-/* flag = 1: all 2*nc half-sweeps of one iteration of every sample in one
- * launch (dataflow sweep, one block per tile), tiles taken sample-major or
- * half-sweep-major; ctl = 4 + ns*L zeroed words of the context, left zeroed
- * by the launch */
+/* flag = 1: all 2*nc half-sweeps of g.fit (>= 1) iterations of every sample
+ * in one launch (dataflow sweep, one block per tile), tiles taken
+ * sample-major or half-sweep-major; the demon walks are not advanced (the
+ * caller adds g.fit afterwards); ctl = 4 + ns*L zeroed words of the context,
+ * left zeroed by the launch */
 cudaError_t micsa_launch_sweep_flow(const micsa_geo &g, int sample_major, uint32_t *spin,
                                     uint32_t *d0, uint32_t *d1, const uint8_t *jb,
                                     const int *walk, unsigned *ctl, cudaStream_t st);
@@ -136,6 +138,8 @@ cudaError_t micsa_launch_gen_rnd(const micsa_geo &g, int p, const uint32_t *te,
 /* walk[s] = (walk[s] + 1) mod L/2 for all samples */
 cudaError_t micsa_launch_walk_advance(const micsa_geo &g, int *walk,
                                       cudaStream_t st);
+/* walk[s] = (walk[s] + n) mod L/2 for the running samples */
+cudaError_t micsa_launch_walk_add(const micsa_geo &g, int *walk, int n, cudaStream_t st);
 
 /* reference-layout words ref[h*nr + r] (one colour, one sample/plane) ->
  * device words dst (colour p base of that plane), demon translation k

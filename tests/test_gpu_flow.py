@@ -17,9 +17,10 @@ from test_gpu_parity import random_state
 pytestmark = pytest.mark.gpu
 
 
-def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1):
+def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1, fit=1):
     env = {"MICSA_SWEEP_ZC": str(zc), "MICSA_SWEEP_PD": str(pd), "MICSA_SWEEP_FLOW": "1",
-           "MICSA_SWEEP_OCC": str(occ), "MICSA_SWEEP_SPLIT": str(split), "MICSA_RESIDENT": "0"}
+           "MICSA_SWEEP_OCC": str(occ), "MICSA_SWEEP_SPLIT": str(split), "MICSA_RESIDENT": "0",
+           "MICSA_FLOW_ITERS": str(fit)}
     if tile:
         env["MICSA_SWEEP_TILE"] = tile
     old = {k: os.environ.get(k) for k in env}
@@ -144,3 +145,52 @@ def test_dataflow_wait_that_runs_out_is_reported_and_the_gpu_stays_usable():
         ctx.iterate(3)
         ctx.synchronize()
         _check(ctx, st, L, nr, nc, 3)
+
+
+@pytest.mark.parametrize("L,nr,nc,ns,zc,fit,iters,split", [
+    (32, 64, 6, 2, 4, 4, 21, 1),    # 5 launches of 4 iterations and one of 1; walks wrap
+    (24, 32, 2, 2, 8, 16, 37, 0),   # 3 slabs, 16 iterations per launch
+    (16, 64, 6, 1, 16, 4, 9, 1),    # one slab
+    (40, 96, 3, 3, 8, 16, 23, 0),   # three word groups
+])
+def test_flow_sweep_several_iterations_per_launch(L, nr, nc, ns, zc, fit, iters, split):
+    """The dataflow sweep carrying several iterations per launch: half-sweep
+    j of the launch is half-sweep j % 2nc of iteration j / 2nc, ordered by the
+    same per-slab rule (which also orders the demon words the walk moves from
+    one iteration to the next); the remainder runs from the one-iteration
+    graph, and micsa_monte_carlo stays one iteration."""
+    ctx = _context(L, nr, ns, nc, zc, 0, 3, None, split, fit)
+    assert "fit=%d" % fit in ctx.tuning(), ctx.tuning()
+    rng = np.random.default_rng(5 * L + fit + ns)
+    st = random_state(rng, L, nr, nc, ns)
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(iters - 1)
+        ctx.monte_carlo(1)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, iters)
+
+
+def test_flow_sweep_several_iterations_frozen_and_headline():
+    """16 iterations per launch with a frozen sample, then the headline
+    shape (L=160, 2 x 64 replicas, whole-row blocks, 8-plane slabs) over one
+    launch of 16 iterations and one more."""
+    L, nr, nc, ns = 32, 64, 4, 3
+    ctx = _context(L, nr, ns, nc, 4, 2, 3, split=1, fit=16)
+    st = random_state(np.random.default_rng(41), L, nr, nc, ns)
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(16)
+        ctx.set_active([1, 0, 1])
+        ctx.iterate(16)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, 32, samples=(0, 2))
+        _check(ctx, st, L, nr, nc, 16, samples=(1,))
+    L, nr, nc, ns = 160, 64, 6, 2
+    ctx = _context(L, nr, ns, nc, 8, 2, 3, "row", fit=16)
+    st = random_state(np.random.default_rng(1600), L, nr, nc, ns)
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(17)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, 17)
