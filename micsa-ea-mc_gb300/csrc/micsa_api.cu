@@ -377,16 +377,23 @@ int autotune(micsa_ctx *ctx) {
       g.tw = tw;
       g.flow = tm == 4;
       g.quad = tm == 5;
-      /* one iteration's half-sweeps in their launch order, captured and
-       * replayed as a graph the way micsa_iterate runs them: timed launch by
-       * launch, small lattices would measure the host's launch rate */
+      /* the dataflow sweep is timed carrying 16 iterations per launch, its
+       * best form (the launch boundary drains the GPU); the count is
+       * settled below for the chosen shape */
+      g.fit = g.flow ? 16 : 1;
+      /* one iteration's half-sweeps (16 for the dataflow sweep) in their
+       * launch order, captured and replayed as a graph the way micsa_iterate
+       * runs them: timed launch by launch, small lattices would measure the
+       * host's launch rate */
       cudaGraph_t gr = nullptr;
       cudaGraphExec_t ge = nullptr;
       MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       cudaError_t le = launch_halves(ctx, g, sp, 0, g.nc, nullptr);
       /* with the walk advancing, as in a run: the x translation of the demon
        * planes misaligns their rows at most shifts, never at shift 0 */
-      if (le == cudaSuccess) le = micsa_launch_walk_advance(g, ctx->walk, ctx->stream);
+      if (le == cudaSuccess)
+        le = g.fit > 1 ? micsa_launch_walk_add(g, ctx->walk, g.fit, ctx->stream)
+                       : micsa_launch_walk_advance(g, ctx->walk, ctx->stream);
       const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &gr);
       MICSA_CK(le);
       MICSA_CK(ce);
@@ -397,12 +404,13 @@ int autotune(micsa_ctx *ctx) {
       cudaError_t te = cudaGraphLaunch(ge, ctx->stream); /* warm-up */
       if (te == cudaSuccess) te = cudaEventRecord(e0, ctx->stream);
       for (int rep = 0; rep < reps && te == cudaSuccess; rep++) te = cudaGraphLaunch(ge, ctx->stream);
+      /* (reps graph replays: reps iterations, or 16 * reps for the dataflow sweep) */
       if (te == cudaSuccess) te = cudaEventRecord(e1, ctx->stream);
       if (te == cudaSuccess) te = cudaEventSynchronize(e1);
       if (te == cudaSuccess) te = cudaEventElapsedTime(&ms, e0, e1);
       cudaGraphExecDestroy(ge);
       MICSA_CK(te);
-      const double per = ms / (2.0 * g.nc * reps);
+      const double per = ms / (2.0 * g.nc * reps * g.fit);
       if (n < MICSA_TUNE_MAX) {
         ctx->tune_zc[n] = g.zc;
         ctx->tune_pd[n] = g.pd;
