@@ -848,21 +848,24 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
     cst[C_PER_SAMPLE] = (unsigned)(g.fit > 1 ? g.fit : 1) * 2u * (unsigned)g.nc * nslab * T;
     cst[C_SMAJ] = (unsigned)smaj;
     dep_take(g, walk, ctl, cst, job);
+    if (pf <= 0) dep_wait(g, ctl, cst, job);
   }
   __syncthreads();
-  /* the tile's demon words are independent of the half-sweep before it:
-   * on their way into L2 while the lead thread waits for the dependencies
-   * (at most pf planes: the z loop's own prefetch takes over from there) */
   /* half-sweep J of the launch is half-sweep J % 2nc of its iteration J / 2nc,
    * whose demons sit one walk step further per iteration */
   const unsigned per_it = 2u * (unsigned)g.nc, J = job[1];
   const unsigned jj = J % per_it;
   const int kwalk = (int)((job[6] + J / per_it) % (unsigned)g.Lh);
-  if (pf > 0 && !micsa_frozen(g, (int)job[0]))
-    prefetch_tile_demons<VW>(g, (int)(jj & 1u), (int)(jj >> 1), job[0], job[5], job[4], job[3],
-                             job[2] * (unsigned)zc, pf < zc ? pf : zc, kwalk, d0, d1);
-  if (lead) dep_wait(g, ctl, cst, job);
-  __syncthreads();
+  if (pf > 0) {
+    /* the tile's demon words are independent of the half-sweep before it:
+     * on their way into L2 while the lead thread waits for the dependencies
+     * (at most pf planes: the z loop's own prefetch takes over from there) */
+    if (!micsa_frozen(g, (int)job[0]))
+      prefetch_tile_demons<VW>(g, (int)(jj & 1u), (int)(jj >> 1), job[0], job[5], job[4],
+                               job[3], job[2] * (unsigned)zc, pf < zc ? pf : zc, kwalk, d0, d1);
+    if (lead) dep_wait(g, ctl, cst, job);
+    __syncthreads();
+  }
   {
     const unsigned s = job[0];
     if (!micsa_frozen(g, (int)s)) {
