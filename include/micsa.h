@@ -33,6 +33,7 @@
  *   MICSA_REFRESH_WPS=n  segment length of the GPU demon refresh, in words
  *   MICSA_REFRESH_OCC=1  the refresh kernel without its register budget
  *   MICSA_FLOW_ITERS=k   iterations per dataflow launch, with a pinned shape
+ *   MICSA_SWEEP_PERS=1   the dataflow sweep's persistent form, with a pinned shape
  *   MICSA_SWEEP_PF=n     the dataflow sweep requests n demon planes of each tile
  *                        into L2 before its dependency wait
  *   MICSA_MULTI_ZC=z     slab depth of the mixed-lattice launch (no timing)
@@ -186,12 +187,14 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
  * pipe: each z step's loads issued one step ahead into registers |
  * flow: the iteration's half-sweeps in one dataflow launch, one block per
  * tile, ordered by per-slab dependency counters; split then orders its
- * tiles sample-major (1) or half-sweep-major (0) | quad: direct loads with
+ * tiles sample-major (1) or half-sweep-major (0) | pflow: the same in its
+ * persistent form, as many blocks as fit the GPU, each looping over tickets
+ * and taking the next during its tile | quad: direct loads with
  * four one-word sites per thread (32 replicas)>
  * tile=<default | row: blocks span whole rows along x>
  * fit=<iterations per launch of the dataflow sweep: its wavefront runs on
  * from one iteration into the next; 1 for the other loads> |
- * <zc>/<pd>/<split>/<occ>/<load 0|1|2|3|4|5>/<tile 0|1>:<ms per half-sweep> ...",
+ * <zc>/<pd>/<split>/<occ>/<load 0|1|2|3|4|5|6 (6: pflow)>/<tile 0|1>:<ms per half-sweep> ...",
  * with " cached" before the "|" when the choice and its table were taken
  * over from an earlier context of the same device, L, nr, samples and nc in
  * this process (MICSA_TUNE_CACHE=0 times every context instead).  The

@@ -237,7 +237,7 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
  * choice and table instead of timing again, so batches and servers that open
  * many contexts of a few shapes pay for each shape once. */
 struct tune_entry {
-  int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, fit, n;
+  int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, fit, pers, n;
   std::vector<int> zcs, pds, splits, occs, loads, tws;
   std::vector<double> ms;
 };
@@ -287,6 +287,7 @@ int autotune(micsa_ctx *ctx) {
     g.tw = ew && !strcmp(ew, "row") && !g.tma && micsa_sweep_wide_differs(g.L, eq && atoi(eq) ? 4 : 2);
     g.flow = ef && atoi(ef) && !g.tma && !g.async && !g.pipe;
     g.quad = eq && atoi(eq) && g.W == 1 && !g.tma && !g.async && !g.pipe && !g.flow;
+    if (const char *ep = getenv("MICSA_SWEEP_PERS")) g.pers = g.flow && atoi(ep) == 1;
     if (const char *ek = getenv("MICSA_FLOW_ITERS")) {
       const int k = atoi(ek);
       if (g.flow && k >= 1 && k <= 64) g.fit = k;
@@ -314,6 +315,7 @@ int autotune(micsa_ctx *ctx) {
       g.flow = t.flow;
       g.quad = t.quad;
       g.fit = t.fit;
+      g.pers = t.pers;
       ctx->ntune = t.n;
       for (int c = 0; c < t.n; c++) {
         ctx->tune_zc[c] = t.zcs[c];
@@ -333,7 +335,8 @@ int autotune(micsa_ctx *ctx) {
   MICSA_CK(cudaEventCreate(&e1));
   double best = 1e30;
   int best_zc = zcs[nz - 1], best_pd = 0, best_split = 0, best_occ = 3, best_tma = 0;
-  int best_async = 0, best_pipe = 0, best_tw = 0, best_flow = 0, best_quad = 0, n = 0;
+  int best_async = 0, best_pipe = 0, best_tw = 0, best_flow = 0, best_quad = 0, best_pers = 0;
+  int n = 0;
   const int ntw = micsa_sweep_wide_differs(g.L) ? 2 : 1, ntw4 = micsa_sweep_wide_differs(g.L, 4) ? 2 : 1;
   /* The dataflow sweep is timed only for large lattices (many slabs per
    * half-sweep, so that its tiles rarely wait): contexts of small lattices
@@ -356,7 +359,7 @@ int autotune(micsa_ctx *ctx) {
    * blocks per SM instead of 3 or 4), 4 direct loads in one dataflow launch
    * per iteration (split: its tiles sample-major or half-sweep-major), 5
    * direct loads with four one-word sites per thread (W = 1) */
-  for (int tm = 0; tm < 6; tm++)
+  for (int tm = 0; tm < 7; tm++)
   for (int tw = 0; tw < (tm == 5 ? ntw4 : ntw); tw++)
   for (int oc = 0; oc < nocc; oc++)
   for (int si = 0; si < nsp; si++)
@@ -366,7 +369,7 @@ int autotune(micsa_ctx *ctx) {
       if (tm == 1 && (!ctx->tma.ok || zcs[c] > 4)) continue; /* staged tiles: <= 4 planes */
       if (tm == 2 && (g.W != 2 || pds[d])) continue;          /* no L2 prefetch there */
       if (tw && (tm == 1 || tm == 2)) continue; /* whole-row blocks: direct and pipelined loads */
-      if ((tm == 4 && !try_flow) || (tm == 5 && g.W != 1)) continue;
+      if (((tm == 4 || tm == 6) && !try_flow) || (tm == 5 && g.W != 1)) continue;
       const int sp = sps[si];
       g.zc = zcs[c];
       g.pd = pds[d];
@@ -375,7 +378,8 @@ int autotune(micsa_ctx *ctx) {
       g.async = tm == 2;
       g.pipe = tm == 3;
       g.tw = tw;
-      g.flow = tm == 4;
+      g.flow = tm == 4 || tm == 6;
+      g.pers = tm == 6;
       g.quad = tm == 5;
       /* the dataflow sweep is timed carrying 16 iterations per launch, its
        * best form (the launch boundary drains the GPU); the count is
@@ -432,6 +436,7 @@ int autotune(micsa_ctx *ctx) {
         best_pipe = g.pipe;
         best_tw = g.tw;
         best_flow = g.flow;
+        best_pers = g.pers;
         best_quad = g.quad;
       }
     }
@@ -445,6 +450,7 @@ int autotune(micsa_ctx *ctx) {
   g.pipe = best_pipe;
   g.tw = best_tw;
   g.flow = best_flow;
+  g.pers = best_pers;
   g.quad = best_quad;
   g.fit = 1;
   if (g.flow) {
@@ -496,6 +502,7 @@ int autotune(micsa_ctx *ctx) {
     t.flow = g.flow;
     t.quad = g.quad;
     t.fit = g.fit;
+    t.pers = g.pers;
     t.n = n;
     t.zcs.assign(ctx->tune_zc, ctx->tune_zc + n);
     t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
@@ -590,6 +597,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.flow = 0;
   g.quad = 0;
   g.fit = 1;
+  g.pers = 0;
   {
     /* MICSA_SWEEP_PF=n: the dataflow sweep requests n demon planes of each
      * tile into L2 before its dependency wait (0: none) */
@@ -679,7 +687,7 @@ int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
   int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s fit=%d%s |", ctx->g.zc,
                    ctx->g.pd, ctx->split, ctx->g.occ,
-                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : (ctx->g.flow ? "flow" : (ctx->g.quad ? "quad" : "direct")))),
+                   ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : (ctx->g.flow ? (ctx->g.pers ? "pflow" : "flow") : (ctx->g.quad ? "quad" : "direct")))),
                    ctx->g.tw ? "row" : "default", ctx->g.flow ? ctx->g.fit : 1,
                    ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)

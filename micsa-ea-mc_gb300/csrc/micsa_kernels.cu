@@ -746,10 +746,8 @@ __device__ __forceinline__ bool flow_wait3(const unsigned *a, const unsigned *b,
  * bx, row tile, group, walk) from the launch's constants in cst[] and wait
  * for the tile's dependencies. */
 enum { C_GX, C_NSLAB, C_T, C_PER_HALF, C_PER_SAMPLE, C_YT, C_SMAJ, C_N };
-__device__ __forceinline__ void dep_take(const micsa_geo &g, const int *__restrict__ walk,
-                                         unsigned *__restrict__ ctl, const unsigned *cst,
-                                         unsigned *job) {
-  const unsigned u = atomicAdd(ctl, 1u);
+__device__ __forceinline__ void dep_decode(const micsa_geo &g, const int *__restrict__ walk,
+                                           const unsigned *cst, const unsigned u, unsigned *job) {
   const unsigned nslab = cst[C_NSLAB], T = cst[C_T], gx = cst[C_GX], ytiles = cst[C_YT];
   unsigned s, j, r2;
   if (cst[C_SMAJ]) {
@@ -771,6 +769,11 @@ __device__ __forceinline__ void dep_take(const micsa_geo &g, const int *__restri
   job[4] = (t / gx) % ytiles;
   job[5] = t / (gx * ytiles);
   job[6] = (unsigned)__ldg(walk + s);
+}
+__device__ __forceinline__ void dep_take(const micsa_geo &g, const int *__restrict__ walk,
+                                         unsigned *__restrict__ ctl, const unsigned *cst,
+                                         unsigned *job) {
+  dep_decode(g, walk, cst, atomicAdd(ctl, 1u), job);
 }
 /* ... and the lead thread's wait for the tile's dependencies */
 __device__ __forceinline__ void dep_wait(const micsa_geo &g, unsigned *__restrict__ ctl,
@@ -884,6 +887,91 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
   }
   __syncthreads();
   if (job[7]) { /* every other block has finished: reset for the next launch */
+    const unsigned tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+    const unsigned n = (unsigned)g.ns * cst[C_NSLAB];
+    for (unsigned k = tid; k < n; k += nt) ctl[4 + k] = 0;
+    if (lead) {
+      ctl[0] = 0;
+      ctl[1] = 0;
+    }
+  }
+}
+
+/* Persistent form of the dataflow sweep: a grid of the blocks that fit the
+ * GPU at once, each looping over tickets.  A block takes its next ticket
+ * while it computes the current tile (the atomic's round trip and the
+ * decode leave the block's barrier path), releases the current tile's slab
+ * counter, then waits for the next tile's dependencies.  Tickets are taken
+ * in order by running blocks and a block holds at most one ticket it has
+ * not started, which is larger than the one it works on; so the smallest
+ * unfinished ticket always belongs to a block that is computing it, with
+ * its dependencies (smaller tickets) done: the launch cannot stall.  Tiles,
+ * order and results are those of k_sweep_dep. */
+template <int VW, bool WIDE, int MINB>
+__global__ void __launch_bounds__(TPB, MINB)
+k_sweep_pdep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, const int zc,
+             const int pd, const int smaj, const unsigned total, uint32_t *__restrict__ spin,
+             uint32_t *__restrict__ d0, uint32_t *__restrict__ d1,
+             const uint8_t *__restrict__ jb, const int *__restrict__ walk,
+             unsigned *__restrict__ ctl) {
+  grid_dependency_sync();
+  __shared__ unsigned cst[C_N];
+  __shared__ unsigned job[2][8]; /* s, j, slab, bx, row tile, group, walk, valid */
+  __shared__ unsigned last;
+  const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+  if (lead) {
+    const unsigned gx = (unsigned)g.Lh / 2u / blockDim.x;
+    const unsigned nslab = (unsigned)(g.L / zc);
+    const unsigned T = gx * (unsigned)ytiles * (unsigned)G;
+    cst[C_GX] = gx;
+    cst[C_NSLAB] = nslab;
+    cst[C_T] = T;
+    cst[C_YT] = (unsigned)ytiles;
+    cst[C_PER_HALF] = nslab * T;
+    cst[C_PER_SAMPLE] = (unsigned)(g.fit > 1 ? g.fit : 1) * 2u * (unsigned)g.nc * nslab * T;
+    cst[C_SMAJ] = (unsigned)smaj;
+    const unsigned u = atomicAdd(ctl, 1u);
+    job[0][7] = u < total;
+    if (u < total) {
+      dep_decode(g, walk, cst, u, job[0]);
+      dep_wait(g, ctl, cst, job[0]);
+    }
+  }
+  __syncthreads();
+  const unsigned per_it = 2u * (unsigned)g.nc;
+  for (int cur = 0; job[cur][7]; cur ^= 1) {
+    unsigned un = 0;
+    if (lead) un = atomicAdd(ctl, 1u); /* the next ticket, used after this tile */
+    {
+      const unsigned *jc = job[cur];
+      const unsigned J = jc[1], jj = J % per_it, s = jc[0];
+      const int kwalk = (int)((jc[6] + J / per_it) % (unsigned)g.Lh);
+      if (!micsa_frozen(g, (int)s)) {
+        micsa_tma none;
+        sweep_block<VW, true, WIDE, false, true>(g, (int)(jj & 1u), (int)(jj >> 1), s, jc[5],
+                                                 jc[4], jc[3], jc[2] * (unsigned)zc, zc, pd,
+                                                 kwalk, spin, d0, d1, jb, nullptr, none);
+      }
+    }
+    __syncthreads();
+    if (lead) {
+      __threadfence();
+      atomicAdd(ctl + 4 + job[cur][0] * cst[C_NSLAB] + job[cur][2], 1u);
+      unsigned *nx = job[cur ^ 1];
+      nx[7] = un < total;
+      if (un < total) {
+        dep_decode(g, walk, cst, un, nx);
+        dep_wait(g, ctl, cst, nx);
+      }
+    }
+    __syncthreads();
+  }
+  if (lead) {
+    __threadfence();
+    last = atomicAdd(ctl + 1, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) { /* every other block has finished: reset for the next launch */
     const unsigned tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
     const unsigned n = (unsigned)g.ns * cst[C_NSLAB];
     for (unsigned k = tid; k < n; k += nt) ctl[4 + k] = 0;
@@ -1901,12 +1989,26 @@ static cudaError_t sweep_vw(const micsa_geo &g, int p, int ic, bool micsa, uint3
   return cudaGetLastError();
 }
 
-/* the dataflow sweep: one block per tile */
+/* the dataflow sweep: one block per tile, or (g.pers) the persistent form
+ * with as many blocks as fit the GPU at once */
 template <int VW, bool WIDE, int MINB>
 static cudaError_t sweep_flow_k(const micsa_geo &g, int smaj, int ytiles, int G, int zc,
                                 dim3 block, int64_t tiles, uint32_t *spin, uint32_t *d0,
                                 uint32_t *d1, const uint8_t *jb, const int *walk, unsigned *ctl,
                                 cudaStream_t st) {
+  if (g.pers) {
+    int dev = 0, nsm = 0, per = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_pdep<VW, WIDE, MINB>,
+                                                        (int)(block.x * block.y), 0);
+    if (e != cudaSuccess) return e;
+    int64_t nb = (int64_t)nsm * (per > 0 ? per : 1);
+    if (nb > tiles) nb = tiles;
+    return launch_sweep(g, k_sweep_pdep<VW, WIDE, MINB>, dim3((unsigned)nb), block, 0, st, g,
+                        ytiles, G, zc, g.pd, smaj, (unsigned)tiles, spin, d0, d1, jb, walk, ctl);
+  }
   return launch_sweep(g, k_sweep_dep<VW, WIDE, MINB>, dim3((unsigned)tiles), block, 0, st, g,
                       ytiles, G, zc, g.pd, smaj, g.pf, spin, d0, d1, jb, walk, ctl);
 }

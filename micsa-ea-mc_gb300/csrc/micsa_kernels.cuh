@@ -40,6 +40,7 @@ struct micsa_geo {
   int pf;     /* dataflow sweep: demon planes of its tile requested into L2 before its
                  dependency wait (0 = none) */
   int fit;    /* dataflow sweep: iterations carried by one launch (>= 1) */
+  int pers;   /* 1: the dataflow sweep in its persistent form (blocks loop over tickets) */
   int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */

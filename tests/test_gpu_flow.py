@@ -17,10 +17,10 @@ from test_gpu_parity import random_state
 pytestmark = pytest.mark.gpu
 
 
-def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1, fit=1):
+def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1, fit=1, pers=0):
     env = {"MICSA_SWEEP_ZC": str(zc), "MICSA_SWEEP_PD": str(pd), "MICSA_SWEEP_FLOW": "1",
            "MICSA_SWEEP_OCC": str(occ), "MICSA_SWEEP_SPLIT": str(split), "MICSA_RESIDENT": "0",
-           "MICSA_FLOW_ITERS": str(fit)}
+           "MICSA_FLOW_ITERS": str(fit), "MICSA_SWEEP_PERS": str(pers)}
     if tile:
         env["MICSA_SWEEP_TILE"] = tile
     old = {k: os.environ.get(k) for k in env}
@@ -33,7 +33,7 @@ def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1, fit=1):
                 os.environ.pop(k, None)
             else:
                 os.environ[k] = v
-    assert "load=flow" in ctx.tuning(), ctx.tuning()
+    assert ("load=pflow" if pers else "load=flow") in ctx.tuning(), ctx.tuning()
     return ctx
 
 
@@ -189,6 +189,44 @@ def test_flow_sweep_several_iterations_frozen_and_headline():
     L, nr, nc, ns = 160, 64, 6, 2
     ctx = _context(L, nr, ns, nc, 8, 2, 3, "row", fit=16)
     st = random_state(np.random.default_rng(1600), L, nr, nc, ns)
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(17)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, 17)
+
+
+@pytest.mark.parametrize("L,nr,nc,ns,zc,occ,fit,split,tile", [
+    (32, 64, 6, 2, 4, 3, 1, 1, None),
+    (32, 64, 6, 3, 4, 4, 4, 0, None),      # 4-block register budget, half-sweep-major
+    (24, 32, 2, 2, 8, 3, 16, 0, None),     # 3 slabs
+    (64, 128, 6, 2, 8, 3, 4, 1, None),     # four-word vectors
+    (40, 96, 3, 3, 8, 3, 16, 1, None),     # three word groups
+    (96, 64, 5, 2, 4, 3, 16, 1, "row"),    # whole-row blocks
+])
+def test_persistent_flow_sweep_matches_oracle(L, nr, nc, ns, zc, occ, fit, split, tile):
+    """The persistent form of the dataflow sweep (blocks loop over tickets,
+    each taking its next ticket during its current tile): same tiles, same
+    order rule, same results -- with one and several iterations per launch,
+    remainders from the one-iteration graph, frozen samples."""
+    ctx = _context(L, nr, ns, nc, zc, 2 if zc > 2 else 0, occ, tile, split, fit, pers=1)
+    rng = np.random.default_rng(11 * L + nr + fit)
+    st = random_state(rng, L, nr, nc, ns)
+    iters = L // 2 + 3
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(iters - 2)
+        ctx.set_active([0] + [1] * (ns - 1))
+        ctx.iterate(2)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, iters, samples=range(1, ns))
+        _check(ctx, st, L, nr, nc, iters - 2, samples=(0,))
+
+
+def test_persistent_flow_sweep_headline_shape():
+    L, nr, nc, ns = 160, 64, 6, 2
+    ctx = _context(L, nr, ns, nc, 8, 2, 3, "row", fit=16, pers=1)
+    st = random_state(np.random.default_rng(1601), L, nr, nc, ns)
     with ctx:
         _upload(ctx, st)
         ctx.iterate(17)
