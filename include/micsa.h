@@ -34,6 +34,7 @@
  *   MICSA_REFRESH_OCC=1  the refresh kernel without its register budget
  *   MICSA_FLOW_ITERS=k   iterations per dataflow launch, with a pinned shape
  *   MICSA_SWEEP_PERS=1   the dataflow sweep's persistent form, with a pinned shape
+ *   MICSA_FLOW_HALF=1    half-height dataflow tiles, with a pinned shape
  *   MICSA_SWEEP_PF=n     the dataflow sweep requests n demon planes of each tile
  *                        into L2 before its dependency wait
  *   MICSA_MULTI_ZC=z     slab depth of the mixed-lattice launch (no timing)
@@ -191,7 +192,8 @@ int micsa_profile(micsa_ctx *ctx, int64_t n, double *sweep_ms, double *iteration
  * persistent form, as many blocks as fit the GPU, each looping over tickets
  * and taking the next during its tile | quad: direct loads with
  * four one-word sites per thread (32 replicas)>
- * tile=<default | row: blocks span whole rows along x>
+ * tile=<default | row: blocks span whole rows along x>[/2: half-height
+ * dataflow tiles]
  * fit=<iterations per launch of the dataflow sweep: its wavefront runs on
  * from one iteration into the next; 1 for the other loads> |
  * <zc>/<pd>/<split>/<occ>/<load 0|1|2|3|4|5|6 (6: pflow)>/<tile 0|1>:<ms per half-sweep> ...",

@@ -237,7 +237,7 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
  * choice and table instead of timing again, so batches and servers that open
  * many contexts of a few shapes pay for each shape once. */
 struct tune_entry {
-  int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, fit, pers, n;
+  int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, fit, pers, half, n;
   std::vector<int> zcs, pds, splits, occs, loads, tws;
   std::vector<double> ms;
 };
@@ -288,6 +288,7 @@ int autotune(micsa_ctx *ctx) {
     g.flow = ef && atoi(ef) && !g.tma && !g.async && !g.pipe;
     g.quad = eq && atoi(eq) && g.W == 1 && !g.tma && !g.async && !g.pipe && !g.flow;
     if (const char *ep = getenv("MICSA_SWEEP_PERS")) g.pers = g.flow && atoi(ep) == 1;
+    if (const char *eh = getenv("MICSA_FLOW_HALF")) g.half = g.flow && !g.pers && atoi(eh) == 1;
     if (const char *ek = getenv("MICSA_FLOW_ITERS")) {
       const int k = atoi(ek);
       if (g.flow && k >= 1 && k <= 64) g.fit = k;
@@ -316,6 +317,7 @@ int autotune(micsa_ctx *ctx) {
       g.quad = t.quad;
       g.fit = t.fit;
       g.pers = t.pers;
+      g.half = t.half;
       ctx->ntune = t.n;
       for (int c = 0; c < t.n; c++) {
         ctx->tune_zc[c] = t.zcs[c];
@@ -486,6 +488,35 @@ int autotune(micsa_ctx *ctx) {
       if (per < best_it) best_it = per, best_fit = k;
     }
     g.fit = best_fit;
+    if (!g.pers) {
+      /* half-height tiles: twice the tiles per slab, each half as long, for a
+       * sweep whose wavefront of dependencies bounds it */
+      g.half = 1;
+      cudaGraph_t gr = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      MICSA_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t le = launch_halves(ctx, g, ctx->split, 0, g.nc, nullptr);
+      if (le == cudaSuccess)
+        le = g.fit > 1 ? micsa_launch_walk_add(g, ctx->walk, g.fit, ctx->stream)
+                       : micsa_launch_walk_advance(g, ctx->walk, ctx->stream);
+      const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &gr);
+      MICSA_CK(le);
+      MICSA_CK(ce);
+      const cudaError_t ie = cudaGraphInstantiate(&ge, gr, 0);
+      cudaGraphDestroy(gr);
+      MICSA_CK(ie);
+      const int rr = g.fit >= 16 ? 1 : (g.fit >= 4 ? 2 : 6);
+      float ms = 0;
+      cudaError_t te = cudaGraphLaunch(ge, ctx->stream);
+      if (te == cudaSuccess) te = cudaEventRecord(e0, ctx->stream);
+      for (int rep = 0; rep < rr && te == cudaSuccess; rep++) te = cudaGraphLaunch(ge, ctx->stream);
+      if (te == cudaSuccess) te = cudaEventRecord(e1, ctx->stream);
+      if (te == cudaSuccess) te = cudaEventSynchronize(e1);
+      if (te == cudaSuccess) te = cudaEventElapsedTime(&ms, e0, e1);
+      cudaGraphExecDestroy(ge);
+      MICSA_CK(te);
+      if (ms / ((double)rr * g.fit) >= best_it) g.half = 0;
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -503,6 +534,7 @@ int autotune(micsa_ctx *ctx) {
     t.quad = g.quad;
     t.fit = g.fit;
     t.pers = g.pers;
+    t.half = g.half;
     t.n = n;
     t.zcs.assign(ctx->tune_zc, ctx->tune_zc + n);
     t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
@@ -598,6 +630,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.quad = 0;
   g.fit = 1;
   g.pers = 0;
+  g.half = 0;
   {
     /* MICSA_SWEEP_PF=n: the dataflow sweep requests n demon planes of each
      * tile into L2 before its dependency wait (0: none) */
@@ -685,10 +718,11 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s fit=%d%s |", ctx->g.zc,
+  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s%s fit=%d%s |", ctx->g.zc,
                    ctx->g.pd, ctx->split, ctx->g.occ,
                    ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : (ctx->g.flow ? (ctx->g.pers ? "pflow" : "flow") : (ctx->g.quad ? "quad" : "direct")))),
-                   ctx->g.tw ? "row" : "default", ctx->g.flow ? ctx->g.fit : 1,
+                   ctx->g.tw ? "row" : "default", ctx->g.flow && ctx->g.half ? "/2" : "",
+                   ctx->g.flow ? ctx->g.fit : 1,
                    ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)
     k += snprintf(buf + k, n - (size_t)k, " %d/%d/%d/%d/%d/%d:%.5fms", ctx->tune_zc[c],

@@ -828,8 +828,8 @@ __device__ __forceinline__ void prefetch_tile_demons(const micsa_geo &g, int p, 
 /* The tile's values go through shared memory and are read where they are
  * used, so that none of them stays in a register across the sweep body
  * (which needs about all of the 64 registers of the 4-blocks budget). */
-template <int VW, bool WIDE, int MINB>
-__global__ void __launch_bounds__(TPB, MINB)
+template <int VW, bool WIDE, int MINB, int BT = TPB>
+__global__ void __launch_bounds__(BT, MINB)
 k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, const int zc,
             const int pd, const int smaj, const int pf, uint32_t *__restrict__ spin,
             uint32_t *__restrict__ d0,
@@ -2009,6 +2009,9 @@ static cudaError_t sweep_flow_k(const micsa_geo &g, int smaj, int ytiles, int G,
     return launch_sweep(g, k_sweep_pdep<VW, WIDE, MINB>, dim3((unsigned)nb), block, 0, st, g,
                         ytiles, G, zc, g.pd, smaj, (unsigned)tiles, spin, d0, d1, jb, walk, ctl);
   }
+  if (g.half) /* half-height tiles: the same registers per thread, twice the blocks per SM */
+    return launch_sweep(g, k_sweep_dep<VW, WIDE, 2 * MINB, TPB / 2>, dim3((unsigned)tiles), block,
+                        0, st, g, ytiles, G, zc, g.pd, smaj, g.pf, spin, d0, d1, jb, walk, ctl);
   return launch_sweep(g, k_sweep_dep<VW, WIDE, MINB>, dim3((unsigned)tiles), block, 0, st, g,
                       ytiles, G, zc, g.pd, smaj, g.pf, spin, d0, d1, jb, walk, ctl);
 }
@@ -2020,6 +2023,7 @@ static cudaError_t sweep_flow_vw(const micsa_geo &g, int smaj, uint32_t *spin, u
   const int G = g.W / VW;
   int tx, ty;
   sweep_tile(g.L, g.tw, &tx, &ty);
+  if (g.half && !g.pers) ty = ty / 2 > 0 ? ty / 2 : 1; /* blocks of tx x ty/2 threads */
   const int ytiles = (g.L + ty - 1) / ty;
   const int zc = g.zc > 0 ? g.zc : 4;
   if (g.L % zc) return cudaErrorInvalidValue;

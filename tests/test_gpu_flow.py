@@ -17,10 +17,10 @@ from test_gpu_parity import random_state
 pytestmark = pytest.mark.gpu
 
 
-def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1, fit=1, pers=0):
+def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1, fit=1, pers=0, half=0):
     env = {"MICSA_SWEEP_ZC": str(zc), "MICSA_SWEEP_PD": str(pd), "MICSA_SWEEP_FLOW": "1",
            "MICSA_SWEEP_OCC": str(occ), "MICSA_SWEEP_SPLIT": str(split), "MICSA_RESIDENT": "0",
-           "MICSA_FLOW_ITERS": str(fit), "MICSA_SWEEP_PERS": str(pers)}
+           "MICSA_FLOW_ITERS": str(fit), "MICSA_SWEEP_PERS": str(pers), "MICSA_FLOW_HALF": str(half)}
     if tile:
         env["MICSA_SWEEP_TILE"] = tile
     old = {k: os.environ.get(k) for k in env}
@@ -232,3 +232,22 @@ def test_persistent_flow_sweep_headline_shape():
         ctx.iterate(17)
         ctx.synchronize()
         _check(ctx, st, L, nr, nc, 17)
+
+
+@pytest.mark.parametrize("L,nr,nc,ns,zc,occ,fit,split,tile", [
+    (32, 64, 6, 2, 4, 3, 4, 1, None),
+    (40, 96, 3, 3, 8, 4, 1, 0, None),
+    (96, 64, 5, 2, 4, 3, 16, 1, "row"),    # whole-row blocks of 3 rows
+])
+def test_flow_sweep_half_height_tiles(L, nr, nc, ns, zc, occ, fit, split, tile):
+    """Half-height dataflow tiles (blocks of about 128 threads, twice as many
+    per SM): the same rule over twice the tiles, same results as the oracle."""
+    ctx = _context(L, nr, ns, nc, zc, 0, occ, tile, split, fit, half=1)
+    assert "/2" in ctx.tuning(), ctx.tuning()
+    st = random_state(np.random.default_rng(7 * L + fit + occ), L, nr, nc, ns)
+    iters = L // 2 + 1
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(iters)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, iters)
