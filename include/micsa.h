@@ -373,8 +373,10 @@ int micsa_server_destroy(micsa_server *sv);
  * MICSA_MULTI_ITERS=k pins it).  The contexts stay usable as before (uploads, refreshes,
  * measurements, run flags); micsa_multi_iterate is ordered after the work
  * queued on every context's stream and before what is queued there next.
- * Results equal micsa_iterate on each context alone.  err (optional)
- * receives a message on failure. */
+ * Results equal micsa_iterate on each context alone.  The contexts must
+ * outlive the mixed launch object (destroy it first); their sample counts and shapes
+ * are fixed, their run flags (micsa_set_active) may change between calls.
+ * err (optional) receives a message on failure. */
 typedef struct micsa_multi micsa_multi;
 int micsa_multi_create(micsa_ctx *const *ctxs, int n, micsa_multi **out, char *err,
                        size_t errlen);
