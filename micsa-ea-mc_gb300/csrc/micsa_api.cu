@@ -44,9 +44,9 @@ struct micsa_ctx {
   std::vector<uint8_t> active_host; /* host copy of the run flags */
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;   /* g.fit iterations (dataflow), else one */
-  cudaGraph_t graph1 = nullptr;
-  cudaGraphExec_t graph1_exec = nullptr;  /* one iteration, when g.fit > 1 */
-  int64_t graph1_launches = 0;
+  std::vector<cudaGraph_t> rem_graph;     /* rem_graph[k]: one launch of k < g.fit iterations */
+  std::vector<cudaGraphExec_t> rem_exec;
+  std::vector<int64_t> rem_launches;
   int64_t launches = 0;
   int resident = 0;        /* small lattice: iterations run in shared memory */
   int split = 0;           /* k > 0: half-sweep launches per group of k samples, group-major
@@ -806,8 +806,10 @@ int micsa_destroy(micsa_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
-  if (ctx->graph1_exec) cudaGraphExecDestroy(ctx->graph1_exec);
-  if (ctx->graph1) cudaGraphDestroy(ctx->graph1);
+  for (cudaGraphExec_t e : ctx->rem_exec)
+    if (e) cudaGraphExecDestroy(e);
+  for (cudaGraph_t gr : ctx->rem_graph)
+    if (gr) cudaGraphDestroy(gr);
   void *bufs[] = {ctx->spin, ctx->dem0,     ctx->dem1,    ctx->rnd,      ctx->jb,
                   ctx->lut,  ctx->te,       ctx->keys,    ctx->walk,     ctx->stage,
                   ctx->acc,  ctx->plan_lcg, ctx->plan_xo, ctx->plan_fib, ctx->rec,
@@ -1157,14 +1159,24 @@ int micsa_iterate(micsa_ctx *ctx, int64_t n) {
   int rc = set_device(ctx);
   if (rc || (rc = ready_for_sweeps(ctx, 1))) return rc;
   /* the graph replays ctx->g.fit iterations at a time (the dataflow sweep may
-   * carry several per launch); a one-iteration graph takes the remainder */
+   * carry several per launch); the remainder k < fit runs as one launch of k
+   * iterations, from a graph made on first use */
   const int unit = ctx->g.flow && ctx->g.fit > 1 ? ctx->g.fit : 1;
   if (!ctx->graph_exec && !ctx->resident &&
       (rc = capture_iterations(ctx, unit, &ctx->graph, &ctx->graph_exec, &ctx->graph_launches)))
     return rc;
-  if (unit > 1 && n % unit && !ctx->graph1_exec &&
-      (rc = capture_iterations(ctx, 1, &ctx->graph1, &ctx->graph1_exec, &ctx->graph1_launches)))
-    return rc;
+  const int left = unit > 1 ? (int)(n % unit) : 0;
+  if (left) {
+    if (ctx->rem_exec.size() < (size_t)unit) {
+      ctx->rem_graph.resize((size_t)unit, nullptr);
+      ctx->rem_exec.resize((size_t)unit, nullptr);
+      ctx->rem_launches.resize((size_t)unit, 0);
+    }
+    if (!ctx->rem_exec[left] &&
+        (rc = capture_iterations(ctx, left, &ctx->rem_graph[left], &ctx->rem_exec[left],
+                                 &ctx->rem_launches[left])))
+      return rc;
+  }
   if (ctx->resident) {
     /* small lattices: whole iterations in shared memory, up to 1024 per launch */
     for (int64_t done = 0; done < n;) {
@@ -1178,11 +1190,10 @@ int micsa_iterate(micsa_ctx *ctx, int64_t n) {
   }
   for (int64_t i = 0; i < n / unit; i++) MICSA_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
   ctx->launches += n / unit * ctx->graph_launches;
-  if (unit > 1)
-    for (int64_t i = 0; i < n % unit; i++) {
-      MICSA_CK(cudaGraphLaunch(ctx->graph1_exec, ctx->stream));
-      ctx->launches += ctx->graph1_launches;
-    }
+  if (left) {
+    MICSA_CK(cudaGraphLaunch(ctx->rem_exec[left], ctx->stream));
+    ctx->launches += ctx->rem_launches[left];
+  }
   return MICSA_OK;
 }
 

@@ -157,8 +157,8 @@ def test_flow_sweep_several_iterations_per_launch(L, nr, nc, ns, zc, fit, iters,
     """The dataflow sweep carrying several iterations per launch: half-sweep
     j of the launch is half-sweep j % 2nc of iteration j / 2nc, ordered by the
     same per-slab rule (which also orders the demon words the walk moves from
-    one iteration to the next); the remainder runs from the one-iteration
-    graph, and micsa_monte_carlo stays one iteration."""
+    one iteration to the next); the remainder runs as one launch of the
+    remaining iterations, and micsa_monte_carlo stays one iteration."""
     ctx = _context(L, nr, ns, nc, zc, 0, 3, None, split, fit)
     assert "fit=%d" % fit in ctx.tuning(), ctx.tuning()
     rng = np.random.default_rng(5 * L + fit + ns)
@@ -208,7 +208,7 @@ def test_persistent_flow_sweep_matches_oracle(L, nr, nc, ns, zc, occ, fit, split
     """The persistent form of the dataflow sweep (blocks loop over tickets,
     each taking its next ticket during its current tile): same tiles, same
     order rule, same results -- with one and several iterations per launch,
-    remainders from the one-iteration graph, frozen samples."""
+    remainders as one launch of the remaining iterations, frozen samples."""
     ctx = _context(L, nr, ns, nc, zc, 2 if zc > 2 else 0, occ, tile, split, fit, pers=1)
     rng = np.random.default_rng(11 * L + nr + fit)
     st = random_state(rng, L, nr, nc, ns)
