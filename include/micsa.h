@@ -35,6 +35,8 @@
  *   MICSA_FLOW_ITERS=k   iterations per dataflow launch, with a pinned shape
  *   MICSA_SWEEP_PERS=1   the dataflow sweep's persistent form, with a pinned shape
  *   MICSA_FLOW_HALF=1    half-height dataflow tiles, with a pinned shape
+ *   MICSA_FLOW_XS=1      the dataflow sweep takes the remaining x-neighbour word
+ *                        from the adjacent lane (warp shuffle), with a pinned shape
  *   MICSA_SWEEP_PF=n     the dataflow sweep requests n demon planes of each tile
  *                        into L2 before its dependency wait
  *   MICSA_MULTI_ZC=z     slab depth of the mixed-lattice launch (no timing)

@@ -237,7 +237,7 @@ cudaError_t launch_halves(micsa_ctx *ctx, const micsa_geo &g, int split, int ic0
  * choice and table instead of timing again, so batches and servers that open
  * many contexts of a few shapes pay for each shape once. */
 struct tune_entry {
-  int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, fit, pers, half, n;
+  int zc, pd, split, occ, tma, async, pipe, tw, flow, quad, fit, pers, half, xs, n;
   std::vector<int> zcs, pds, splits, occs, loads, tws;
   std::vector<double> ms;
 };
@@ -289,6 +289,8 @@ int autotune(micsa_ctx *ctx) {
     g.quad = eq && atoi(eq) && g.W == 1 && !g.tma && !g.async && !g.pipe && !g.flow;
     if (const char *ep = getenv("MICSA_SWEEP_PERS")) g.pers = g.flow && atoi(ep) == 1;
     if (const char *eh = getenv("MICSA_FLOW_HALF")) g.half = g.flow && !g.pers && atoi(eh) == 1;
+    if (const char *ex = getenv("MICSA_FLOW_XS"))
+      g.xs = g.flow && !g.pers && !g.half && atoi(ex) == 1;
     if (const char *ek = getenv("MICSA_FLOW_ITERS")) {
       const int k = atoi(ek);
       if (g.flow && k >= 1 && k <= 64) g.fit = k;
@@ -318,6 +320,7 @@ int autotune(micsa_ctx *ctx) {
       g.fit = t.fit;
       g.pers = t.pers;
       g.half = t.half;
+      g.xs = t.xs;
       ctx->ntune = t.n;
       for (int c = 0; c < t.n; c++) {
         ctx->tune_zc[c] = t.zcs[c];
@@ -344,8 +347,10 @@ int autotune(micsa_ctx *ctx) {
    * half-sweep, so that its tiles rarely wait): contexts of small lattices
    * run side by side in batches and servers, where blocks that wait on
    * dependencies hold SM slots the other contexts' kernels need (the batched
-   * mixed-L stream lost 30% with it).  MICSA_SWEEP_FLOW=0 leaves it out
-   * everywhere. */
+   * mixed-L stream lost 30% with it).  Alone it loses as well below L=128,
+   * where a half-sweep has too few slabs for tiles to find work ahead (L=64 x 8
+   * samples: 1.30 against 7.02 attempts/ps; L=96 x 16: 3.85 against 6.75).
+   * MICSA_SWEEP_FLOW=0 leaves it out everywhere. */
   const char *ef0 = getenv("MICSA_SWEEP_FLOW");
   const bool try_flow = !(ef0 && !strcmp(ef0, "0")) && g.L >= 128;
   const int reps = 3;
@@ -594,6 +599,7 @@ int autotune(micsa_ctx *ctx) {
     t.fit = g.fit;
     t.pers = g.pers;
     t.half = g.half;
+    t.xs = g.xs;
     t.n = n;
     t.zcs.assign(ctx->tune_zc, ctx->tune_zc + n);
     t.pds.assign(ctx->tune_pd, ctx->tune_pd + n);
@@ -690,6 +696,7 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
   g.fit = 1;
   g.pers = 0;
   g.half = 0;
+  g.xs = 0;
   {
     /* MICSA_SWEEP_PF=n: the dataflow sweep requests n demon planes of each
      * tile into L2 before its dependency wait (0: none) */
@@ -777,10 +784,11 @@ int micsa_create(const micsa_config *cfg, micsa_ctx **out) {
 
 int micsa_tuning_report(const micsa_ctx *ctx, char *buf, size_t n) {
   if (!ctx || !buf || n == 0) return MICSA_ERR_ARG;
-  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s%s fit=%d%s |", ctx->g.zc,
+  int k = snprintf(buf, n, "zc=%d pd=%d split=%d occ=%d load=%s tile=%s%s%s fit=%d%s |", ctx->g.zc,
                    ctx->g.pd, ctx->split, ctx->g.occ,
                    ctx->g.tma ? "tma" : (ctx->g.async ? "async" : (ctx->g.pipe ? "pipe" : (ctx->g.flow ? (ctx->g.pers ? "pflow" : "flow") : (ctx->g.quad ? "quad" : "direct")))),
                    ctx->g.tw ? "row" : "default", ctx->g.flow && ctx->g.half ? "/2" : "",
+                   ctx->g.flow && ctx->g.xs ? "+xs" : "",
                    ctx->g.flow ? ctx->g.fit : 1,
                    ctx->tune_cached ? " cached" : "");
   for (int c = 0; c < ctx->ntune && k > 0 && (size_t)k < n; c++)

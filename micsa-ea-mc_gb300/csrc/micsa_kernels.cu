@@ -392,7 +392,8 @@ __device__ __forceinline__ void st_u32(uint32_t *a, uint32_t v, uint64_t pol) {
 /* LIN: the thread's row and x/2 pair come from the caller (tile = y,
  * bx = pair index), not from the block shape -- the mixed-lattice launch
  * maps a fixed block onto consecutive (row, pair) units of any L. */
-template <int VW, bool MICSA, bool WIDE, bool TMA, bool FLOW, int S = 2, bool LIN = false>
+template <int VW, bool MICSA, bool WIDE, bool TMA, bool FLOW, int S = 2, bool LIN = false,
+          bool XS = false>
 __device__ __forceinline__ void sweep_block(
     const micsa_geo &g, const int p, const int ic, const uint32_t s, const uint32_t grp,
     const uint32_t tile, const uint32_t bx, const uint32_t z0, const int zc, const int pd,
@@ -401,10 +402,18 @@ __device__ __forceinline__ void sweep_block(
     const micsa_tma &tm) {
   static_assert(S == 2 || (S == 4 && VW == 1 && WIDE && !TMA), "four sites: one word each");
   static_assert(!(LIN && TMA), "TMA staging needs the block-shaped tile");
+  static_assert(!XS || (S == 2 && !LIN && !TMA), "x halo by shuffle: pairs, block-shaped tiles");
   constexpr int N = S * VW; /* words per thread and plane */
   using PR = typename sites_io<VW, WIDE, S>::type;
   const uint32_t L = g.L, Lh = g.Lh, W = g.W;
   const uint32_t y = LIN ? tile : tile * blockDim.y + threadIdx.y;
+  /* XS: the lanes of this warp that stay (rows inside the lattice) */
+  unsigned xs_mask = 0;
+  if (XS) {
+    const unsigned lin = threadIdx.y * blockDim.x + threadIdx.x;
+    const unsigned in_warp = blockDim.x * blockDim.y - (lin & ~31u);
+    xs_mask = __ballot_sync(in_warp >= 32 ? 0xffffffffu : (1u << in_warp) - 1u, y < L);
+  }
   if (y >= L) return;
   const uint32_t xa = S * (LIN ? bx : bx * blockDim.x + threadIdx.x); /* x/2 of the first site */
   const uint32_t plane = L * Lh;
@@ -503,8 +512,23 @@ __device__ __forceinline__ void sweep_block(
   PR::template ld_oth<FLOW>(oth + ((z0 == 0 ? L - 1 : z0 - 1) * plane + row) * W, W, vm, keep);
   PR::template ld_oth<FLOW>(oth + (z0 * plane + row) * W, W, v0, keep);
 
+  /* XS: the remaining x neighbour is a word the adjacent thread of the row
+   * holds in v0 -- its first site's words when the row looks at +x, its
+   * second site's at -x (rowoff is the same along a row) -- taken by shuffle
+   * when that thread is in the same warp, loaded otherwise (row ends, the
+   * periodic wrap, warp boundaries).  Source lane (bits 0-4) and "taken"
+   * (bit 5) per direction, -x in bits 0-7 and +x in bits 8-15: */
+  uint32_t xs_code = 0;
+  if (XS) {
+    const unsigned lin = threadIdx.y * blockDim.x + threadIdx.x;
+    const bool okp = threadIdx.x + 1 < blockDim.x && xa + S < Lh && ((lin + 1) & 31u) != 0;
+    const bool okm = threadIdx.x > 0 && xa > 0 && (lin & 31u) != 0;
+    xs_code = (((okm ? lin - 1 : lin) & 31u) | (okm ? 32u : 0u)) |
+              ((((okp ? lin + 1 : lin) & 31u) | (okp ? 32u : 0u)) << 8);
+  }
+
   uint32_t zdd = zd;
-#pragma unroll 2
+#pragma unroll(XS ? 1 : 2) /* XS: unrolled twice it spills at 80 registers */
   for (uint32_t t = 0; t < (uint32_t)zc; t++) {
     const uint32_t z = z0 + t;
     const uint32_t zo = z * plane;
@@ -514,10 +538,20 @@ __device__ __forceinline__ void sweep_block(
     PR::template ld_oth<FLOW>(oth + ((z + 1 == L ? 0 : zo + plane) + row) * W, W, up, keep);
     PR::template ld_oth<FLOW>(oth + (zo + rowN) * W, W, vn, keep);
     PR::template ld_oth<FLOW>(oth + (zo + rowS) * W, W, vs, keep);
-    if (FLOW)
-      hint<VW>::ld_co(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
-    else
-      hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
+    bool ext_done = false;
+    if (XS) {
+      const uint32_t c = xs_code >> (8 * rowoff);
+      ext_done = (c & 32u) != 0;
+#pragma unroll
+      for (int w = 0; w < VW; w++)
+        ext[w] = __shfl_sync(xs_mask, rowoff ? v0[w] : v0[VW + w], (int)(c & 31u));
+    }
+    if (!ext_done) {
+      if (FLOW)
+        hint<VW>::ld_co(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
+      else
+        hint<VW>::ld_nc(oth + (zo + (rowoff ? rowXp : rowXm)) * W, ext, keep);
+    }
     const uint32_t jbs = S == 4 ? ld_u32_keep(jbp + zo + row, keep) : ld_u16_keep(jbp + zo + row, keep);
     bool from_smem = false;
     if (TMA && staged) {
@@ -828,7 +862,7 @@ __device__ __forceinline__ void prefetch_tile_demons(const micsa_geo &g, int p, 
 /* The tile's values go through shared memory and are read where they are
  * used, so that none of them stays in a register across the sweep body
  * (which needs about all of the 64 registers of the 4-blocks budget). */
-template <int VW, bool WIDE, int MINB, int BT = TPB>
+template <int VW, bool WIDE, int MINB, int BT = TPB, bool XS = false>
 __global__ void __launch_bounds__(BT, MINB)
 k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, const int zc,
             const int pd, const int smaj, const int pf, uint32_t *__restrict__ spin,
@@ -873,9 +907,9 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
     const unsigned s = job[0];
     if (!micsa_frozen(g, (int)s)) {
       micsa_tma none;
-      sweep_block<VW, true, WIDE, false, true>(g, (int)(jj & 1u), (int)(jj >> 1), s, job[5],
-                                               job[4], job[3], job[2] * (unsigned)zc, zc, pd,
-                                               kwalk, spin, d0, d1, jb, nullptr, none);
+      sweep_block<VW, true, WIDE, false, true, 2, false, XS>(
+          g, (int)(jj & 1u), (int)(jj >> 1), s, job[5], job[4], job[3], job[2] * (unsigned)zc,
+          zc, pd, kwalk, spin, d0, d1, jb, nullptr, none);
     }
   }
   __syncthreads();
@@ -2011,6 +2045,9 @@ static cudaError_t sweep_flow_k(const micsa_geo &g, int smaj, int ytiles, int G,
   }
   if (g.half) /* half-height tiles: the same registers per thread, twice the blocks per SM */
     return launch_sweep(g, k_sweep_dep<VW, WIDE, 2 * MINB, TPB / 2>, dim3((unsigned)tiles), block,
+                        0, st, g, ytiles, G, zc, g.pd, smaj, g.pf, spin, d0, d1, jb, walk, ctl);
+  if (g.xs) /* the x halo by warp shuffle */
+    return launch_sweep(g, k_sweep_dep<VW, WIDE, MINB, TPB, true>, dim3((unsigned)tiles), block,
                         0, st, g, ytiles, G, zc, g.pd, smaj, g.pf, spin, d0, d1, jb, walk, ctl);
   return launch_sweep(g, k_sweep_dep<VW, WIDE, MINB>, dim3((unsigned)tiles), block, 0, st, g,
                       ytiles, G, zc, g.pd, smaj, g.pf, spin, d0, d1, jb, walk, ctl);

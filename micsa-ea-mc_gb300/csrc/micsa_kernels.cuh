@@ -43,6 +43,8 @@ struct micsa_geo {
   int pers;   /* 1: the dataflow sweep in its persistent form (blocks loop over tickets) */
   int half;   /* 1: the dataflow sweep with half-height tiles (blocks of about 128
                  threads, twice as many per SM) */
+  int xs;     /* 1: the dataflow sweep takes the remaining x-neighbour word from the
+                 adjacent lane by warp shuffle instead of loading it */
   int s0;     /* context index of this launch's first sample (per-sample launches) */
   const uint8_t *active; /* device flags [ns]: 0 = sample frozen (skipped by the
                             sweeps, the walk and the measurements); null = all */

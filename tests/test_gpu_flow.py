@@ -17,10 +17,11 @@ from test_gpu_parity import random_state
 pytestmark = pytest.mark.gpu
 
 
-def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1, fit=1, pers=0, half=0):
+def _context(L, nr, ns, nc, zc, pd=0, occ=3, tile=None, split=1, fit=1, pers=0, half=0, xs=0):
     env = {"MICSA_SWEEP_ZC": str(zc), "MICSA_SWEEP_PD": str(pd), "MICSA_SWEEP_FLOW": "1",
            "MICSA_SWEEP_OCC": str(occ), "MICSA_SWEEP_SPLIT": str(split), "MICSA_RESIDENT": "0",
-           "MICSA_FLOW_ITERS": str(fit), "MICSA_SWEEP_PERS": str(pers), "MICSA_FLOW_HALF": str(half)}
+           "MICSA_FLOW_ITERS": str(fit), "MICSA_SWEEP_PERS": str(pers), "MICSA_FLOW_HALF": str(half),
+           "MICSA_FLOW_XS": str(xs)}
     if tile:
         env["MICSA_SWEEP_TILE"] = tile
     old = {k: os.environ.get(k) for k in env}
@@ -245,6 +246,28 @@ def test_flow_sweep_half_height_tiles(L, nr, nc, ns, zc, occ, fit, split, tile):
     ctx = _context(L, nr, ns, nc, zc, 0, occ, tile, split, fit, half=1)
     assert "/2" in ctx.tuning(), ctx.tuning()
     st = random_state(np.random.default_rng(7 * L + fit + occ), L, nr, nc, ns)
+    iters = L // 2 + 1
+    with ctx:
+        _upload(ctx, st)
+        ctx.iterate(iters)
+        ctx.synchronize()
+        _check(ctx, st, L, nr, nc, iters)
+
+
+@pytest.mark.parametrize("L,nr,nc,ns,zc,occ,fit,split,tile", [
+    (32, 64, 6, 2, 4, 3, 4, 1, None),      # x blocks narrower than a row: block edges
+    (40, 96, 3, 3, 8, 4, 1, 0, None),      # one-word groups; rows past L in the last tile
+    (96, 64, 5, 2, 4, 3, 16, 1, "row"),    # 24 threads a row: rows straddle warps
+    (64, 128, 6, 2, 8, 3, 4, 1, "row"),    # four-word vectors, 16 threads a row
+    (24, 32, 2, 2, 8, 3, 2, 0, "row"),     # 6 threads a row, one word
+])
+def test_flow_sweep_x_halo_by_shuffle(L, nr, nc, ns, zc, occ, fit, split, tile):
+    """The dataflow sweep taking the remaining x-neighbour word from the
+    adjacent lane (warp shuffle) and loading it only at row ends, the periodic
+    wrap and warp boundaries: same results as the oracle."""
+    ctx = _context(L, nr, ns, nc, zc, 0, occ, tile, split, fit, xs=1)
+    assert "+xs" in ctx.tuning(), ctx.tuning()
+    st = random_state(np.random.default_rng(11 * L + fit + occ), L, nr, nc, ns)
     iters = L // 2 + 1
     with ctx:
         _upload(ctx, st)
