@@ -272,7 +272,7 @@ def run_micsa(a, dist):
             "frac": round(achieved / peak, 4), "peak_kind": kind,
             "algorithmic_bytes_per_launch": int(per_launch),
             "launch_ms": round(sweep_ms, 5), "iteration_ms_profiled": round(iter_ms, 5),
-            "autotune": ctx.tuning(),
+            "autotune": _tuning_summary(ctx.tuning()),
             "traffic": traffic, "traffic_source": tnote}
     # ---- end to end through the C ABI with host buffers
     e2e = None
@@ -282,6 +282,22 @@ def run_micsa(a, dist):
     ctx.close()
     return dict(value=value, ms=ms, roof=roof, clocks=ck, e2e=e2e, launches=launches,
                 attempts=attempts)
+
+
+def _tuning_summary(t):
+    """The chosen launch shape, the number of candidates timed and the three
+    fastest (zc/pd/split/occ/load/tile: ms per half-sweep)."""
+    head, _, rest = t.partition("|")
+    cands = []
+    for c in rest.split():
+        shape, _, ms = c.partition(":")
+        try:
+            cands.append((float(ms.rstrip("ms")), shape))
+        except ValueError:
+            pass
+    cands.sort()
+    best = " ".join("%s:%.5fms" % (sh, ms) for ms, sh in cands[:3])
+    return "%s | %d candidates timed%s" % (head.strip(), len(cands), (", fastest " + best) if best else "")
 
 
 def _pinned(arr):
