@@ -32,6 +32,9 @@
  *   MICSA_PDL=0          plain launches instead of programmatic dependent launch
  *   MICSA_REFRESH_WPS=n  segment length of the GPU demon refresh, in words
  *   MICSA_REFRESH_OCC=1  the refresh kernel without its register budget
+ *   MICSA_REFRESH_AHEAD=0|1  refreshes asked for ahead: drawn in place at the
+ *                        commit (0) or at once on the side stream (1); default:
+ *                        in place for contexts on the dataflow sweep
  *   MICSA_FLOW_ITERS=k   iterations per dataflow launch, with a pinned shape
  *   MICSA_SWEEP_PERS=1   the dataflow sweep's persistent form, with a pinned shape
  *   MICSA_FLOW_HALF=1    half-height dataflow tiles, with a pinned shape
@@ -132,7 +135,13 @@ int micsa_refresh_wait(micsa_ctx *ctx);
  * InitWalkers thread (main.cu:340-377).  micsa_refresh_commit makes them
  * current (ordered after the draw and after the work already queued: a
  * device copy, and the walks of those samples reset).  One refresh may be
- * pending at a time.  No counterpart in the reference. */
+ * pending at a time.  A context on the dataflow sweep (large lattices, which
+ * fill the GPU) instead records the draw -- its start states are taken and
+ * the caller's structs advanced now, as above -- and micsa_refresh_commit
+ * draws it in place on the context's stream: the two kernels side by side
+ * are slower than one after the other there, and no copy is needed
+ * (MICSA_REFRESH_AHEAD overrides the choice).  The demons, spins and
+ * structs are the same either way.  No counterpart in the reference. */
 int micsa_refresh_demons_ahead(micsa_ctx *ctx, int first, int count, void *prc, void *xo,
                                const uint64_t *thr);
 int micsa_refresh_commit(micsa_ctx *ctx);
@@ -166,7 +175,11 @@ int micsa_measure(micsa_ctx *ctx, int32_t *e_spin, uint64_t *e_demon,
                   int64_t *q, int64_t *c4);
 
 /* State of one sample back in the reference layouts (copy_from_GPU_for_write,
- * main.cu:473-490).  Demons are returned in the frame of the current walk. */
+ * main.cu:473-490).  Demons are returned in the frame of the current walk.
+ * When both host buffers are page-locked and mapped (cudaHostAlloc,
+ * cudaHostRegister with mapping), the conversion kernels write them directly
+ * across the host link; other buffers are filled from a device staging
+ * buffer.  The results are the same either way. */
 int micsa_download_spins(micsa_ctx *ctx, int sample, uint64_t *even,
                          uint64_t *odd);
 int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0,

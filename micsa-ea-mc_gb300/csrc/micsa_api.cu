@@ -73,6 +73,11 @@ struct micsa_ctx {
   cudaEvent_t ahead_done = nullptr;  /* the draw into the back buffer is done */
   cudaEvent_t commit_done = nullptr; /* the back buffer has been copied out */
   int ahead_first = 0, ahead_count = 0; /* pending drawn-ahead samples (count 0: none) */
+  /* a pending refresh recorded but not drawn yet (drawn in place at the
+   * commit): its records are in rec_b, its jump plan is (def_nw, def_wps) */
+  int ahead_deferred = 0, def_wps = 0;
+  int64_t def_nw = 0;
+  uint64_t def_thr[3] = {0, 0, 0};
   std::thread advancer;              /* host advance of the last refresh's streams */
   char err[512] = {0};
 };
@@ -154,6 +159,20 @@ int ensure_stage(micsa_ctx *ctx) {
   if (ctx->stage) return MICSA_OK;
   MICSA_CK(cudaMalloc(&ctx->stage, ctx->stage_words * sizeof(uint64_t)));
   return MICSA_OK;
+}
+
+/* The device address of a caller's host buffer that kernels may write
+ * directly (page-locked and mapped, as cudaHostAlloc and mapped registered
+ * memory are), else nullptr.  A download into such a buffer converts
+ * straight into it across the host link: one pass at link speed instead of a
+ * conversion into the staging buffer and then a copy. */
+uint64_t *device_view(uint64_t *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError(); /* not a pointer the runtime knows: the staged path */
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? (uint64_t *)a.devicePointer : nullptr;
 }
 
 int ready_for_sweeps(micsa_ctx *ctx, int need_demons) {
@@ -956,9 +975,28 @@ int micsa_refresh_wait(micsa_ctx *ctx) {
 
 namespace {
 
+/* Whether a refresh asked for ahead is drawn at once on the side stream or
+ * recorded and drawn in place on the context's stream at the commit.  A
+ * context whose sweep is the dataflow kernel fills the GPU, and a draw
+ * beside it slows both: L=160 x 2 samples, a 20-iteration job with 6
+ * refreshes took 59.4 ms drawn ahead (whose commit also copies the demon
+ * planes) against 56.6 ms drawn in place.  MICSA_REFRESH_AHEAD=1 keeps the
+ * side stream for every context, =0 defers for every context. */
+bool refresh_deferred(const micsa_ctx *ctx) {
+  if (const char *e = getenv("MICSA_REFRESH_AHEAD")) return atoi(e) == 0;
+  return ctx->g.flow != 0;
+}
+
+int refresh_occ() {
+  const char *e = getenv("MICSA_REFRESH_OCC"); /* 1: the unconstrained-register variant */
+  return e && atoi(e) == 1 ? 1 : 6;
+}
+
 /* One refresh of samples first .. first+count-1: drawn on the context's
  * stream into the current demons (ahead = 0), or on the side stream into
- * the back buffer (ahead = 1, made current by micsa_refresh_commit). */
+ * the back buffer (ahead = 1, made current by micsa_refresh_commit), or
+ * (ahead = 1 and refresh_deferred) recorded, to be drawn in place by
+ * micsa_refresh_commit. */
 int refresh_into(micsa_ctx *ctx, int first, int count, void *prc, void *xo, const uint64_t *thr,
                  int ahead) {
   if (!ctx || !prc || !xo || !thr) return fail(ctx, MICSA_ERR_ARG, "null argument");
@@ -1011,7 +1049,8 @@ int refresh_into(micsa_ctx *ctx, int first, int count, void *prc, void *xo, cons
     MICSA_CK(cudaHostAlloc(&ctx->rec_host, words * sizeof(uint64_t), cudaHostAllocDefault));
     ctx->rec_words = words;
   }
-  if (ahead) {
+  const bool defer = ahead && refresh_deferred(ctx);
+  if (ahead && !defer) {
     const size_t dw = (size_t)ctx->cfg.nsamples * 2 * g.nc * g.P * g.W;
     if (!ctx->side) {
       /* the draw ahead fills what the sweeps leave idle: lowest priority */
@@ -1027,8 +1066,12 @@ int refresh_into(micsa_ctx *ctx, int first, int count, void *prc, void *xo, cons
     MICSA_CK(cudaStreamWaitEvent(ctx->side, ctx->commit_done, 0));
     if (!ctx->back0) MICSA_CK(cudaMalloc(&ctx->back0, 4 * dw));
     if (!ctx->back1) MICSA_CK(cudaMalloc(&ctx->back1, 4 * dw));
+  }
+  if (ahead) {
     if (ctx->rec_b_words < words) {
-      MICSA_CK(cudaStreamSynchronize(ctx->side));
+      /* a committed draw may still read the old records */
+      MICSA_CK(cudaStreamSynchronize(ctx->stream));
+      if (ctx->side) MICSA_CK(cudaStreamSynchronize(ctx->side));
       if (ctx->rec_b) cudaFree(ctx->rec_b);
       ctx->rec_b = nullptr;
       ctx->rec_b_words = 0;
@@ -1036,7 +1079,7 @@ int refresh_into(micsa_ctx *ctx, int first, int count, void *prc, void *xo, cons
       ctx->rec_b_words = words;
     }
   }
-  cudaStream_t st = ahead ? ctx->side : ctx->stream;
+  cudaStream_t st = ahead && !defer ? ctx->side : ctx->stream;
   uint64_t *drec = ahead ? ctx->rec_b : ctx->rec;
   if (!ctx->rec_copied) MICSA_CK(cudaEventCreateWithFlags(&ctx->rec_copied, cudaEventDisableTiming));
 
@@ -1061,16 +1104,22 @@ int refresh_into(micsa_ctx *ctx, int first, int count, void *prc, void *xo, cons
   if ((rc = ensure_refresh_plan(ctx, nw, wps))) return rc;
   MICSA_CK(cudaMemcpyAsync(drec, rec, words * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
   MICSA_CK(cudaEventRecord(ctx->rec_copied, st));
-  micsa_geo gr = g;
-  {
-    const char *e = getenv("MICSA_REFRESH_OCC"); /* 1: the unconstrained-register variant */
-    gr.occ = e && atoi(e) == 1 ? 1 : 6;
+  if (!defer) {
+    micsa_geo gr = g;
+    gr.occ = refresh_occ();
+    MICSA_CK(micsa_launch_refresh(gr, first, count, nw, wps, ctx->plan.nseg, drec, ctx->plan_lcg,
+                                  ctx->plan_xo, ctx->plan_fib, thr, ahead ? ctx->back0 : ctx->dem0,
+                                  ahead ? ctx->back1 : ctx->dem1, st));
+    ctx->launches++;
   }
-  MICSA_CK(micsa_launch_refresh(gr, first, count, nw, wps, ctx->plan.nseg, drec, ctx->plan_lcg,
-                                ctx->plan_xo, ctx->plan_fib, thr, ahead ? ctx->back0 : ctx->dem0,
-                                ahead ? ctx->back1 : ctx->dem1, st));
-  ctx->launches++;
-  if (ahead) {
+  if (defer) { /* drawn in place by micsa_refresh_commit */
+    ctx->ahead_deferred = 1;
+    ctx->def_nw = nw;
+    ctx->def_wps = wps;
+    for (int k = 0; k < 3; k++) ctx->def_thr[k] = thr[k];
+    ctx->ahead_first = first;
+    ctx->ahead_count = count;
+  } else if (ahead) {
     MICSA_CK(cudaEventRecord(ctx->ahead_done, ctx->side));
     ctx->ahead_first = first;
     ctx->ahead_count = count;
@@ -1113,14 +1162,28 @@ int micsa_refresh_commit(micsa_ctx *ctx) {
   int rc = set_device(ctx);
   if (rc) return rc;
   const micsa_geo &g = ctx->g;
-  const size_t per = 2 * (size_t)g.nc * g.P * g.W; /* words per sample and plane type */
-  const size_t off = (size_t)ctx->ahead_first * per, n = (size_t)ctx->ahead_count * per;
-  MICSA_CK(cudaStreamWaitEvent(ctx->stream, ctx->ahead_done, 0));
-  MICSA_CK(cudaMemcpyAsync(ctx->dem0 + off, ctx->back0 + off, 4 * n, cudaMemcpyDeviceToDevice,
-                           ctx->stream));
-  MICSA_CK(cudaMemcpyAsync(ctx->dem1 + off, ctx->back1 + off, 4 * n, cudaMemcpyDeviceToDevice,
-                           ctx->stream));
-  MICSA_CK(cudaEventRecord(ctx->commit_done, ctx->stream));
+  if (ctx->ahead_deferred) {
+    /* the recorded draw, in place, after the work already queued (the plan
+     * is rebuilt only if a refresh of another size came in between) */
+    if ((rc = ensure_refresh_plan(ctx, ctx->def_nw, ctx->def_wps))) return rc;
+    micsa_geo gr = g;
+    gr.occ = refresh_occ();
+    MICSA_CK(micsa_launch_refresh(gr, ctx->ahead_first, ctx->ahead_count, ctx->def_nw,
+                                  ctx->def_wps, ctx->plan.nseg, ctx->rec_b, ctx->plan_lcg,
+                                  ctx->plan_xo, ctx->plan_fib, ctx->def_thr, ctx->dem0, ctx->dem1,
+                                  ctx->stream));
+    ctx->launches++;
+    ctx->ahead_deferred = 0;
+  } else {
+    const size_t per = 2 * (size_t)g.nc * g.P * g.W; /* words per sample and plane type */
+    const size_t off = (size_t)ctx->ahead_first * per, n = (size_t)ctx->ahead_count * per;
+    MICSA_CK(cudaStreamWaitEvent(ctx->stream, ctx->ahead_done, 0));
+    MICSA_CK(cudaMemcpyAsync(ctx->dem0 + off, ctx->back0 + off, 4 * n,
+                             cudaMemcpyDeviceToDevice, ctx->stream));
+    MICSA_CK(cudaMemcpyAsync(ctx->dem1 + off, ctx->back1 + off, 4 * n,
+                             cudaMemcpyDeviceToDevice, ctx->stream));
+    MICSA_CK(cudaEventRecord(ctx->commit_done, ctx->stream));
+  }
   MICSA_CK(cudaMemsetAsync(ctx->walk + ctx->ahead_first, 0, ctx->ahead_count * sizeof(int),
                            ctx->stream));
   for (int s = ctx->ahead_first; s < ctx->ahead_first + ctx->ahead_count; s++) ctx->have_dem[s] = 1;
@@ -1247,14 +1310,18 @@ int micsa_download_spins(micsa_ctx *ctx, int sample, uint64_t *even, uint64_t *o
   if (rc || (rc = set_device(ctx)) || (rc = ensure_stage(ctx))) return rc;
   const micsa_geo &g = ctx->g;
   const int64_t n = g.H * g.nr;
+  uint64_t *dv[2] = {device_view(even), device_view(odd)};
+  const bool direct = dv[0] && dv[1];
   for (int p = 0; p < 2; p++) {
     MICSA_CK(micsa_launch_to_ref(g, p, 0, nullptr, sample,
                                  ctx->spin + ((int64_t)sample * 2 + p) * g.P * g.W,
-                                 ctx->stage + p * n, ctx->stream));
+                                 direct ? dv[p] : ctx->stage + p * n, ctx->stream));
     ctx->launches++;
   }
-  MICSA_CK(cudaMemcpyAsync(even, ctx->stage, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
-  MICSA_CK(cudaMemcpyAsync(odd, ctx->stage + n, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  if (!direct) {
+    MICSA_CK(cudaMemcpyAsync(even, ctx->stage, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    MICSA_CK(cudaMemcpyAsync(odd, ctx->stage + n, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  }
   MICSA_CK(cudaStreamSynchronize(ctx->stream));
   return MICSA_OK;
 }
@@ -1267,16 +1334,19 @@ int micsa_download_demons(micsa_ctx *ctx, int sample, uint64_t *w0, uint64_t *w1
   const int64_t plane = g.H * g.nr, n = 2 * g.nc * plane;
   const uint32_t *src[2] = {ctx->dem0, ctx->dem1};
   uint64_t *dst[2] = {w0, w1};
+  uint64_t *dv[2] = {device_view(w0), device_view(w1)};
+  const bool direct = dv[0] && dv[1];
   for (int k = 0; k < 2; k++) {
     for (int p = 0; p < 2; p++)
       for (int ic = 0; ic < g.nc; ic++) {
         const int64_t pi = (int64_t)p * g.nc + ic;
         MICSA_CK(micsa_launch_to_ref(g, p, ic, ctx->walk, sample,
                                      src[k] + ((int64_t)sample * 2 * g.nc + pi) * g.P * g.W,
-                                     ctx->stage + pi * plane, ctx->stream));
+                                     (direct ? dv[k] : ctx->stage) + pi * plane, ctx->stream));
         ctx->launches++;
       }
-    MICSA_CK(cudaMemcpyAsync(dst[k], ctx->stage, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (!direct)
+      MICSA_CK(cudaMemcpyAsync(dst[k], ctx->stage, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
   }
   MICSA_CK(cudaStreamSynchronize(ctx->stream));
   return MICSA_OK;

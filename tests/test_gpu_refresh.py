@@ -185,10 +185,14 @@ def test_gpu_refresh_async_overlaps_and_matches():
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
-def test_gpu_refresh_ahead_equals_in_place():
-    """Refreshes drawn ahead on the side stream while iterations run, then
-    committed, give the demons, spins and stream structs of in-place
-    refreshes at the same points; committing with nothing pending fails."""
+@pytest.mark.parametrize("mode", ["1", "0"])
+def test_gpu_refresh_ahead_equals_in_place(monkeypatch, mode):
+    """Refreshes asked for ahead -- drawn on the side stream while iterations
+    run (MICSA_REFRESH_AHEAD=1), or recorded and drawn in place at the commit
+    (0, the form for contexts on the dataflow sweep) -- then committed, give
+    the demons, spins and stream structs of in-place refreshes at the same
+    points; committing with nothing pending fails."""
+    monkeypatch.setenv("MICSA_REFRESH_AHEAD", mode)
     L, nr, nc, ns = 16, 64, 3, 2
     thr = micsa.thresholds(BETA)
     H, V = (L // 4) ** 3 // 2, L ** 3
