@@ -392,8 +392,11 @@ __device__ __forceinline__ void st_u32(uint32_t *a, uint32_t v, uint64_t pol) {
 /* LIN: the thread's row and x/2 pair come from the caller (tile = y,
  * bx = pair index), not from the block shape -- the mixed-lattice launch
  * maps a fixed block onto consecutive (row, pair) units of any L. */
+/* UNR: the z loop unrolled UNR times (2 lets the loads of one step overlap
+ * the arithmetic of the other; at 64 registers or fewer per thread the
+ * second step's registers spill, and 1 is faster) */
 template <int VW, bool MICSA, bool WIDE, bool TMA, bool FLOW, int S = 2, bool LIN = false,
-          bool XS = false>
+          bool XS = false, int UNR = 2>
 __device__ __forceinline__ void sweep_block(
     const micsa_geo &g, const int p, const int ic, const uint32_t s, const uint32_t grp,
     const uint32_t tile, const uint32_t bx, const uint32_t z0, const int zc, const int pd,
@@ -528,7 +531,7 @@ __device__ __forceinline__ void sweep_block(
   }
 
   uint32_t zdd = zd;
-#pragma unroll(XS ? 1 : 2) /* XS: unrolled twice it spills at 80 registers */
+#pragma unroll(UNR)
   for (uint32_t t = 0; t < (uint32_t)zc; t++) {
     const uint32_t z = z0 + t;
     const uint32_t zo = z * plane;
@@ -869,6 +872,11 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
             uint32_t *__restrict__ d0,
             uint32_t *__restrict__ d1, const uint8_t *__restrict__ jb,
             const int *__restrict__ walk, unsigned *__restrict__ ctl) {
+  /* the z loop unrolled once where two steps' registers do not fit: pairs
+   * of two-word sites at 64 registers per thread (16-byte spills against 32
+   * unrolled twice; L=160: 8.34 against 8.16 attempts/ps) and the shuffle
+   * form (which spills unrolled twice at 80) */
+  constexpr int UNR = (XS || (VW >= 2 && 65536 / (MINB * BT) <= 64)) ? 1 : 2;
   grid_dependency_sync();
   __shared__ unsigned cst[C_N];
   __shared__ unsigned job[8]; /* s, j, slab, bx, row tile, group, walk, last */
@@ -907,7 +915,7 @@ k_sweep_dep(const __grid_constant__ micsa_geo g, const int ytiles, const int G, 
     const unsigned s = job[0];
     if (!micsa_frozen(g, (int)s)) {
       micsa_tma none;
-      sweep_block<VW, true, WIDE, false, true, 2, false, XS>(
+      sweep_block<VW, true, WIDE, false, true, 2, false, XS, UNR>(
           g, (int)(jj & 1u), (int)(jj >> 1), s, job[5], job[4], job[3], job[2] * (unsigned)zc,
           zc, pd, kwalk, spin, d0, d1, jb, nullptr, none);
     }
