@@ -377,8 +377,10 @@ def e2e_job(a, dist, ctx, hm, attempts):
             "h2d_bytes_per_step": int(h2d // a.steps), "d2h_bytes_per_step": int(d2h // a.steps),
             "ms_per_step": round(te * 1e3 / a.steps, 4), "job_ms": round(te * 1e3, 2),
             "refreshes": nref, "measurements": nmeas,
-            "step": "job of `steps` iterations: state upload, GPU demon refresh (drawn ahead on a "
-                    "side stream) + energy readback at t=0,1,2,4,..., final spins+demons readback"}
+            "step": "job of `steps` iterations: state upload, GPU demon refresh (asked for ahead; "
+                    "drawn in place at each commit for contexts on the dataflow sweep, else on a "
+                    "side stream) + energy readback at t=0,1,2,4,..., final spins+demons readback "
+                    "into pinned buffers"}
 
 
 def e2e_upload_every_step(a, dist, ctx, demons, attempts):
