@@ -1174,6 +1174,10 @@ int micsa_refresh_commit(micsa_ctx *ctx) {
                                   ctx->stream));
     ctx->launches++;
     ctx->ahead_deferred = 0;
+    /* a later draw on the side stream rewrites rec_b only after this one */
+    if (!ctx->commit_done)
+      MICSA_CK(cudaEventCreateWithFlags(&ctx->commit_done, cudaEventDisableTiming));
+    MICSA_CK(cudaEventRecord(ctx->commit_done, ctx->stream));
   } else {
     const size_t per = 2 * (size_t)g.nc * g.P * g.W; /* words per sample and plane type */
     const size_t off = (size_t)ctx->ahead_first * per, n = (size_t)ctx->ahead_count * per;
