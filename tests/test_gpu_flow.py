@@ -68,6 +68,7 @@ def _check(ctx, st, L, nr, nc, iters, samples=None):
     (32, 32, 1, 4, 16, 0, 4, None, 0),    # nc = 1, 2 slabs
     (40, 96, 3, 3, 2, 0, 3, None, 1),
     (96, 64, 5, 2, 4, 2, 3, "row", 0),
+    (32, 256, 6, 1, 4, 0, 3, None, 1),    # two word groups of four-word vectors
 ])
 def test_flow_sweep_matches_oracle(L, nr, nc, ns, zc, pd, occ, tile, split):
     ctx = _context(L, nr, ns, nc, zc, pd, occ, tile, split)

@@ -51,6 +51,8 @@ def test_gpu_reproduces_reference(golden):
     (8, 32, 6, 1, 9), (8, 64, 2, 3, 5), (16, 32, 6, 2, 17), (16, 96, 3, 1, 4),
     (24, 32, 6, 1, 13), (32, 64, 6, 2, 3), (40, 32, 4, 1, 21), (48, 128, 6, 1, 2),
     (64, 64, 6, 1, 2), (64, 64, 6, 8, 3), (96, 32, 6, 2, 2), (56, 64, 5, 3, 4),
+    (24, 256, 3, 1, 5),   # two word groups of four-word vectors
+    (24, 160, 2, 2, 4),   # five word groups of one word
 ])
 def test_gpu_matches_oracle_random_state(L, nr, nc, ns, iters):
     """Arbitrary states (not reachable from seeds), many iterations so the
