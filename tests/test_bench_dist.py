@@ -71,6 +71,20 @@ def test_roofline_traffic_comes_from_the_profile_of_the_tuned_kernel():
     assert bench.traffic_per_launch(160, 64, 2, "no_such_kernel") == (None, None)
 
 
+def test_autotune_summary_keeps_the_pick_and_the_fastest_candidates():
+    """The bench line carries the tuner's pick, how many candidates it timed
+    and the three fastest, not the whole list (hundreds at L=160)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    t = ("zc=8 pd=2 split=1 occ=4 load=flow tile=row fit=16 | 4/0/0/3/0/0:0.04516ms "
+         "8/2/1/4/4/1:0.03152ms 8/2/1/3/4/1:0.03223ms 16/0/0/3/0/0:0.05557ms")
+    got = bench._tuning_summary(t)
+    assert got.startswith("zc=8 pd=2 split=1 occ=4 load=flow tile=row fit=16 | 4 candidates timed")
+    assert got.endswith("fastest 8/2/1/4/4/1:0.03152ms 8/2/1/3/4/1:0.03223ms 4/0/0/3/0/0:0.04516ms")
+    assert bench._tuning_summary("zc=4 pd=0 split=0 occ=3 load=direct tile=default fit=1 cached |") \
+        == "zc=4 pd=0 split=0 occ=3 load=direct tile=default fit=1 cached | 0 candidates timed"
+
+
 def test_reference_arm_never_maps_the_product_library(tmp_path):
     """The reference arm times the CPU restatement only: after a whole
     `bench.py --impl reference` run in one process, libmicsa must not be among
